@@ -1,0 +1,130 @@
+/*
+ * qrdm_gb300.h -- C ABI of libqrdm_gb300.so: QR with Deviation Maximization
+ * pivoting (DM-QR) and companions on one NVIDIA GB300 (sm_103a).
+ *
+ * Drop-in for the C entry points of mdessole/qrdm: same argument lists,
+ * argument meaning and return convention (0 success, -1 invalid argument,
+ * the reference's LAPACKE codes where it has them).  Plain C types only;
+ * "host" pointers are ordinary CPU memory, "device" pointers are CUDA
+ * global-memory addresses on the current device.
+ *
+ * Positive return codes are device-side failures the reference cannot
+ * have (QRDM_ERR_*).  Calls are synchronous with respect to the host and
+ * serialised by an internal lock.
+ */
+#ifndef QRDM_GB300_H_
+#define QRDM_GB300_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QRDM_COL_MAJOR 102 /* LAPACK_COL_MAJOR: the only layout accepted   */
+#define QRDM_ROW_MAJOR 101 /* rejected with -1 (the reference indexes column-
+                                     major internally whatever the flag says) */
+
+/* positive error codes (device-side failures) */
+#define QRDM_ERR_CUDA 1001        /* a CUDA runtime call failed                   */
+#define QRDM_ERR_TIMEOUT 1002     /* a bounded device wait gave up                */
+#define QRDM_ERR_UNSUPPORTED 1003 /* size beyond the device path (nb > 128, ...)  */
+#define QRDM_ERR_NOMEM 1004       /* device allocation failed                     */
+#define QRDM_ERR_INTERNAL 1005    /* a device consistency check failed            */
+/* negative codes kept from the reference */
+#define QRDM_ERR_NAN (-13) /* NaN in the input (reference dlarfb check, src/dlarfb.c:90-92) */
+
+/* Arithmetic of the trailing update (the dominant cost). */
+#define QRDM_PREC_FP64 0  /* native FP64 everywhere                           */
+#define QRDM_PREC_MIXED 1 /* Ozaki-split FP64 emulation on BF16 tensor cores  */
+
+typedef struct qrdm_options {
+  int precision;      /* QRDM_PREC_FP64 (default) or QRDM_PREC_MIXED             */
+  int kstop;          /* > 0: stop once >= kstop columns are triangularised      */
+  int nancheck;       /* 1 (default): scan the input for NaN, return -13         */
+  int slices;         /* Ozaki slices per operand (0 = default 7)                */
+  double gram_margin; /* mixed Gram: |cos| within this of delta is recomputed in
+                         FP64 (0 = default)                                      */
+  int reserved[8];
+} qrdm_options;
+
+typedef struct qrdm_stats {
+  int nblocks;      /* DM blocks (entries written to ncols)                     */
+  int recomputes;   /* partial norms recomputed from scratch                   */
+  int rechecks;     /* cosines re-evaluated in FP64 (mixed Gram)               */
+  int columns;      /* columns triangularised                                  */
+  int launches;     /* kernels launched by the call                            */
+  int timing;       /* in: 1 = record per-phase device times (CUDA events)     */
+  double ms_total;  /* device time of the factorisation                        */
+  double ms_select; /* phase times (timing = 1): DM selection incl. swaps      */
+  double ms_panel;  /*   Householder panels                                    */
+  double ms_tfactor;/*   T factors                                             */
+  double ms_trail;  /*   trailing block-reflector updates                      */
+  double ms_norm;   /*   partial-norm downdates / recomputes                   */
+  double trail_flops; /* algorithmic flops of the trailing updates, 4 m' n' k  */
+  double reserved[5];
+} qrdm_stats;
+
+/* Fill *opt with the defaults (FP64, no kstop, NaN scan on). */
+void qrdm_default_options(qrdm_options* opt);
+
+/* ---------------------------------------------------------------- DM-QR */
+/* Replaces dgeqrdm, include/QRDM.h:19-22 (src/dgeqrdm.c:5-16 ->
+ * src/dgeqrdm_work.c:420-838).  Host pointers, modified in place:
+ *   a      m x n column-major, leading dim lda >= m; on exit R (upper) and
+ *          the Householder vectors (below the diagonal)
+ *   jpvt   n ints; in: nonzero = fixed leading column; out: 1-based
+ *          permutation (column j of A*P was column jpvt[j] of A)
+ *   tau    min(m, n) reflector scalars (entries past the last factored
+ *          column are left untouched, like the reference)
+ *   ncols  n ints; in: ncols[0] = stop mode (0 off, 1: eta = eps*n,
+ *          2: eta = eps*sqrt(n), 3: eta = thres[2]); out: DM block sizes,
+ *          later entries untouched
+ *   thres  [delta, tau_, (eta)]
+ *   nb     maximum DM block (candidates cap), 1 <= nb <= 128 on this device */
+int dgeqrdm(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau,
+            int* ncols, double* thres, int nb);
+
+/* dgeqrdm with options (precision, kstop, NaN scan) and statistics.
+ * opt and stats may be NULL. */
+int dgeqrdm_ex(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau,
+               int* ncols, double* thres, int nb, const qrdm_options* opt, qrdm_stats* stats);
+
+/* dgeqrdm_ex on device-resident data: a, jpvt, tau are DEVICE pointers
+ * (no host copies); ncols and thres stay host pointers. */
+int dgeqrdm_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt, double* d_tau,
+                int* ncols, const double* thres, int nb, const qrdm_options* opt,
+                qrdm_stats* stats);
+
+/* ------------------------------------------------------------------ QP3 */
+/* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot
+ * per column by largest partial norm, first index on ties; jpvt[j] != 0
+ * marks a fixed leading column).  Host pointers. */
+int dgeqp3(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau);
+/* dgeqp3 on device-resident a, jpvt, tau. */
+int dgeqp3_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt, double* d_tau);
+
+/* -------------------------------------------------- unpivoted QR, apply Q */
+/* The LAPACK calls behind the reference's Python QRF and DORMQR
+ * (QRDM_wrapper.c:44-66 LAPACKE_dgeqrf; QRDM_wrapper.c:104-126
+ * LAPACKE_dormqr with side 'L', trans 'N'): C <- Q C with
+ * Q = H(1)...H(k) stored in a/tau.  Host pointers. */
+int qrdm_dgeqrf(int matrix_layout, int m, int n, double* a, int lda, double* tau);
+int qrdm_dormqr(int matrix_layout, int m, int n, int k, const double* a, int lda,
+                const double* tau, double* c, int ldc);
+/* The same on device-resident data. */
+int qrdm_dgeqrf_dev(int matrix_layout, int m, int n, double* d_a, int lda, double* d_tau);
+int qrdm_dormqr_dev(int matrix_layout, int m, int n, int k, const double* d_a, int lda,
+                    const double* d_tau, double* d_c, int ldc);
+
+/* ------------------------------------------------------------- runtime */
+/* Make subsequent calls run on this cudaStream_t (NULL: the library's own
+ * stream).  Returns 0. */
+int qrdm_set_stream(void* stream);
+/* Human-readable build identification. */
+const char* qrdm_version(void);
+/* Release the cached device workspace of the current device. */
+int qrdm_release_workspace(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* QRDM_GB300_H_ */

@@ -1,0 +1,730 @@
+// api.cu -- host driver and C ABI of libqrdm_gb300.
+//
+// The blocked DM-QR loop of dgeqrdm_work (src/dgeqrdm_work.c:694-787) runs
+// on one GPU: every step of a DM block is a kernel on one stream; the host
+// reads back a 64-byte block record (fjb_cmp, max partial norm, error flags)
+// once per block to advance the column pointer and evaluate the stop test.
+// Device workspace is cached per device and grown on demand.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "../../include/qrdm_gb300.h"
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace qrdm {
+
+// ------------------------------------------------------------ workspace
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t b = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) cap = b;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct Ctx {
+  int dev = -1;
+  int nsm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t user = nullptr;
+  bool user_set = false;
+  Buf a, jpvt, tau;                        // device copies for host entry points
+  Buf nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st;
+  Buf pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
+  BlockState* h_st = nullptr;              // pinned host copy of the block record
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ph[8] = {};
+  cudaStream_t stream() const { return user_set ? user : own; }
+};
+
+static std::mutex g_mu;
+static Ctx g_ctx[16];
+static bool g_attr_done[16];
+
+#define CK(x)                                      \
+  do {                                             \
+    cudaError_t _e = (x);                          \
+    if (_e != cudaSuccess) {                       \
+      fprintf(stderr, "qrdm_gb300: %s failed: %s (%s:%d)\n", #x, cudaGetErrorString(_e), __FILE__, __LINE__); \
+      return _e == cudaErrorMemoryAllocation ? QRDM_ERR_NOMEM : QRDM_ERR_CUDA; \
+    }                                              \
+  } while (0)
+
+static int ctx_get(Ctx** out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 16) return QRDM_ERR_UNSUPPORTED;
+  Ctx& c = g_ctx[dev];
+  if (c.dev < 0) {
+    c.dev = dev;
+    CK(cudaDeviceGetAttribute(&c.nsm, cudaDevAttrMultiProcessorCount, dev));
+    int optin = 0;
+    CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    c.smem_optin = (size_t)optin;
+    CK(cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking));
+    CK(cudaHostAlloc((void**)&c.h_st, sizeof(BlockState), cudaHostAllocDefault));
+    CK(cudaEventCreate(&c.ev0));
+    CK(cudaEventCreate(&c.ev1));
+    for (auto& e : c.ph) CK(cudaEventCreate(&e));
+  }
+  if (!g_attr_done[dev]) {
+    int big = (int)c.smem_optin;
+    CK(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
+    CK(cudaFuncSetAttribute(k_topk_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkTile * (int)sizeof(Cand)));
+    CK(cudaFuncSetAttribute(k_topk_final, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkFinal * (int)sizeof(Cand)));
+    CK(cudaFuncSetAttribute(k_dm_pick, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
+    CK(cudaFuncSetAttribute(k_permute_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
+    CK(cudaFuncSetAttribute(k_larft, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 2048));
+    CK(cudaFuncSetAttribute(k_trail_w_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
+    g_attr_done[dev] = true;
+  }
+  *out = &c;
+  return 0;
+}
+
+static int g_launches = 0;  // kernels launched by the current call (under g_mu)
+
+static int check_launch() {
+  ++g_launches;
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    fprintf(stderr, "qrdm_gb300: kernel launch failed: %s\n", cudaGetErrorString(e));
+    return QRDM_ERR_CUDA;
+  }
+  return 0;
+}
+
+// ----------------------------------------------------- one DM-QR instance
+struct DmqrProblem {
+  int m, n, lda, nb;
+  double* A;     // device
+  int* jpvt;     // device, 1-based on exit
+  double* tau;   // device
+  int* ncols;    // host
+  double delta, tau_rel, eta;
+  int stop_mode, kstop, nancheck, precision;
+};
+
+#define RET(x)                 \
+  do {                         \
+    int _r = (x);              \
+    if (_r) return _r;         \
+  } while (0)
+
+static int read_state(Ctx& c, cudaStream_t s) {
+  CK(cudaMemcpyAsync(c.h_st, c.st.p, sizeof(BlockState), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+static double bits_to_double(unsigned long long b) {
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+}
+
+// Panel geometry: G CTAs of R rows; returns false if the slab won't fit.
+static bool panel_geometry(const Ctx& c, int mloc, int kmax, int* G, int* R, size_t* smem) {
+  int g = std::max(1, std::min(c.nsm, ceil_div(mloc, 64)));
+  int r = ceil_div(mloc, g);
+  size_t bytes = (size_t)r * kmax * sizeof(double);
+  if (bytes + 8192 > c.smem_optin) return false;
+  *G = g;
+  *R = r;
+  *smem = bytes;
+  return true;
+}
+
+// C <- op(H) C with H = I - V T V^T for the k = st->fjb_cmp reflectors of
+// V (mloc rows); T must already be in c.T (ldt = kmax).  trans = 1: H^T.
+static int apply_block_reflector(Ctx& c, cudaStream_t s, const double* V, long long ldv, double* C,
+                                 long long ldc, int mloc, int ncols, int c_off_from_fjb, int trans,
+                                 int kmax, const BlockState* d_st) {
+  if (ncols <= 0 || mloc <= 0) return 0;
+  const int nsm = c.nsm;
+  int ntiles = ceil_div(ncols, 64);
+  int nsplit = std::max(1, std::min(std::min(64, ceil_div(2 * nsm, ntiles)), ceil_div(mloc, 128)));
+  CK(c.wpart.ensure(sizeof(double) * (size_t)nsplit * 128 * ntiles * 64));
+  CK(c.w2.ensure(sizeof(double) * (size_t)128 * ntiles * 64));
+  TrailArgs ta;
+  ta.V = V;
+  ta.ldv = ldv;
+  ta.C = C;
+  ta.ldc = ldc;
+  ta.mloc = mloc;
+  ta.ncols = ncols;
+  ta.c_off_from_fjb = c_off_from_fjb;
+  ta.st = d_st;
+  ta.T = c.T.as<double>();
+  ta.ldt = kmax;
+  ta.Wpart = c.wpart.as<double>();
+  ta.W2 = c.w2.as<double>();
+  ta.ldw = ntiles * 64;
+  ta.rows_per_split = ceil_div(mloc, nsplit);
+  ta.trans = trans;
+  const int KT = kmax <= 64 ? 64 : 128;
+  launch_trail_w_partial(KT, dim3(ntiles, nsplit), s, ta);
+  RET(check_launch());
+  size_t rsm = sizeof(double) * ((size_t)KT * 64 + (size_t)KT * KT);
+  k_trail_w_reduce<<<ntiles, 256, rsm, s>>>(ta, nsplit, KT);
+  RET(check_launch());
+  k_trail_update<<<dim3(ntiles, ceil_div(mloc, 64)), 256, 0, s>>>(ta);
+  RET(check_launch());
+  return 0;
+}
+
+// T factor of the k = st->fjb_cmp stored reflectors of V into c.T (ldt = kmax).
+static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv, int mloc,
+                         const double* tau, int kmax, const BlockState* d_st) {
+  int nchunk = std::max(1, std::min(c.nsm, ceil_div(mloc, 256)));
+  int rpc = ceil_div(mloc, nchunk);
+  CK(c.vtv_part.ensure(sizeof(double) * (size_t)std::max(nchunk, c.nsm) * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.T.ensure(sizeof(double) * (size_t)kmax * kmax));
+  k_vtv_stored<<<nchunk, 256, 0, s>>>(V, ldv, mloc, rpc, d_st, c.vtv_part.as<double>());
+  RET(check_launch());
+  int npair = kmax * (kmax - 1) / 2;
+  k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), nchunk, d_st, c.vtv.as<double>());
+  RET(check_launch());
+  k_larft<<<1, 256, sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), tau, d_st, c.T.as<double>(), kmax);
+  RET(check_launch());
+  return 0;
+}
+
+static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
+  cudaStream_t s = c.stream();
+  const bool timing = stats && stats->timing;
+  double ph_ms[5] = {0, 0, 0, 0, 0};
+  double trail_flops = 0.0;
+#define PH(i)                                   \
+  do {                                          \
+    if (timing) CK(cudaEventRecord(c.ph[i], s)); \
+  } while (0)
+  const int m = P.m, n = P.n, nb = P.nb;
+  const long long lda = P.lda;
+  const int minmn = std::min(m, n);
+  const int kcap = std::min(nb, minmn);
+  const int KM = kcap <= 64 ? 64 : 128;
+  const int nsm = c.nsm;
+
+  // ---- workspace
+  int ntile1 = ceil_div(n, kTopkTile);
+  CK(c.nrm.ensure(sizeof(double) * 2 * (size_t)n));
+  CK(c.list.ensure(sizeof(int) * (size_t)n));
+  CK(c.cand_a.ensure(sizeof(Cand) * (size_t)std::max(1, ntile1) * kcap + 64));
+  CK(c.cand_b.ensure(sizeof(Cand) * (size_t)std::max(1, ceil_div(ntile1 * kcap, kTopkTile)) * kcap + 64));
+  CK(c.cand.ensure(sizeof(Cand) * (size_t)KM));
+  const int max_chunks = 2 * nsm;
+  CK(c.gram_part.ensure(sizeof(double) * (size_t)max_chunks * KM * KM));
+  CK(c.gram.ensure(sizeof(double) * (size_t)KM * KM));
+  const int maxsw = 2 * kcap + 2;
+  CK(c.perm.ensure(sizeof(int2) * (size_t)(2 * maxsw)));
+  CK(c.st.ensure(sizeof(BlockState)));
+  CK(c.pan_part.ensure(sizeof(double) * 2 * (size_t)nsm * (QRDM_NB_MAX + 1)));
+  CK(c.pan_row.ensure(sizeof(double) * 2 * (QRDM_NB_MAX + 2)));
+  CK(c.pan_bar.ensure(sizeof(unsigned) * 4));
+  CK(c.vtv_part.ensure(sizeof(double) * (size_t)nsm * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.T.ensure(sizeof(double) * (size_t)KM * KM));
+
+  CK(c.wpart.ensure(sizeof(double) * (size_t)(2 * nsm + ceil_div(n, 64)) * 128 * 64));
+  CK(c.w2.ensure(sizeof(double) * (size_t)128 * ceil_div(n, 64) * 64));
+
+  BlockState* d_st = c.st.as<BlockState>();
+  double* nrm = c.nrm.as<double>();
+  double* nrm_exact = nrm + n;
+
+  CK(cudaEventRecord(c.ev0, s));
+  // ---- norm init (src/dgeqrdm_work.c:672-684) + NaN detection
+  const int nfxd = 0;
+  CK(cudaMemsetAsync(d_st, 0, sizeof(BlockState), s));
+  {
+    int ncol = n - nfxd;
+    int blocks = std::min(ceil_div(ncol, 8), 8 * nsm);
+    k_colnorm_init<<<blocks, 256, 0, s>>>(P.A, lda, nfxd, m - nfxd, nfxd, ncol, nrm + nfxd,
+                                          nrm_exact + nfxd, d_st);
+    RET(check_launch());
+  }
+  RET(read_state(c, s));
+  if (P.nancheck && c.h_st->nnan > 0) return QRDM_ERR_NAN;
+  double maxnrm = bits_to_double(c.h_st->maxnrm_bits);
+  double eta = P.eta * maxnrm;
+
+  int j = nfxd, it = 0, recomputes = 0;
+  while (j < minmn) {
+    const int mloc = m - j, nloc = n - j;
+    const int kmax = std::min(std::min(nb, mloc), nloc);
+    CK(cudaMemsetAsync(d_st, 0, sizeof(BlockState), s));
+    PH(0);
+    // ---- DM candidates (DM_perm :345-351)
+    {
+      const Cand* src = nullptr;
+      int count = nloc;
+      Cand* bufs[2] = {c.cand_a.as<Cand>(), c.cand_b.as<Cand>()};
+      int which = 0;
+      int tiles = ceil_div(count, kTopkTile);
+      k_topk_tile<<<tiles, 1024, kTopkTile * sizeof(Cand), s>>>(nrm + j, nullptr, count, kmax, bufs[which]);
+      RET(check_launch());
+      src = bufs[which];
+      count = tiles * kmax;
+      while (count > kTopkFinal) {
+        which ^= 1;
+        tiles = ceil_div(count, kTopkTile);
+        k_topk_tile<<<tiles, 1024, kTopkTile * sizeof(Cand), s>>>(nullptr, src, count, kmax, bufs[which]);
+        RET(check_launch());
+        src = bufs[which];
+        count = tiles * kmax;
+      }
+      k_topk_final<<<1, 1024, kTopkFinal * sizeof(Cand), s>>>(src, count, kmax, P.tau_rel, c.cand.as<Cand>(), d_st);
+      RET(check_launch());
+    }
+    // ---- cosine matrix (DM_perm :365-379)
+    const int km = kmax <= 64 ? 64 : 128;
+    {
+      int rows_per_chunk = std::max(32, ceil_div(mloc, max_chunks));
+      int nchunk = ceil_div(mloc, rows_per_chunk);
+      launch_gram_partial(km, nchunk, s, P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
+                          c.gram_part.as<double>());
+      RET(check_launch());
+      k_gram_reduce<<<ceil_div(km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
+      RET(check_launch());
+    }
+    // ---- greedy pick + permute_marked (DM_perm :382-415)
+    {
+      int msw = 2 * kmax + 2;
+      size_t smem = sizeof(double) * 2 * msw + sizeof(int) * (2 * msw + 2 * kmax + 2 * msw) +
+                    sizeof(unsigned) * (size_t)ceil_div(nloc, 32) + 64;
+      if (smem + 1024 > c.smem_optin) return QRDM_ERR_UNSUPPORTED;
+      k_dm_pick<<<1, 256, smem, s>>>(c.cand.as<Cand>(), c.gram.as<double>(), km, nloc, kmax, P.delta,
+                                     P.jpvt + j, nrm + j, c.perm.as<int2>(), d_st);
+      RET(check_launch());
+      int max_entries = 2 * msw;
+      size_t psm = sizeof(double) * 32 * (size_t)max_entries;
+      k_permute_columns<<<ceil_div(m, 32), 256, psm, s>>>(P.A, lda, m, j, c.perm.as<int2>(), d_st, max_entries);
+      RET(check_launch());
+    }
+    PH(1);
+    // ---- panel dgeqr2_mia (src/dgeqr2.c) with early exit
+    int G = 1, R = 1;
+    size_t psmem = 0;
+    if (!panel_geometry(c, mloc, kmax, &G, &R, &psmem)) return QRDM_ERR_UNSUPPORTED;
+    {
+      CK(cudaMemsetAsync(c.pan_bar.p, 0, sizeof(unsigned) * 4, s));
+      PanelArgs pa;
+      pa.A = P.A;
+      pa.lda = lda;
+      pa.j = j;
+      pa.mloc = mloc;
+      pa.tau_rel = P.tau_rel;
+      pa.tau = P.tau + j;
+      pa.nrm = nrm + j;
+      pa.st = d_st;
+      pa.part = c.pan_part.as<double>();
+      pa.rowbuf = c.pan_row.as<double>();
+      pa.bar = c.pan_bar.as<unsigned>();
+      pa.vtv_part = c.vtv_part.as<double>();
+      pa.rows_per_cta = R;
+      pa.allow_exit = 1;
+      void* args[] = {&pa};
+      CK(cudaLaunchCooperativeKernel((void*)k_panel, dim3(G), dim3(256), args, psmem, s));
+      ++g_launches;
+    }
+    PH(2);
+    // ---- T factor (dlarft 'F','C', src/dgeqrdm_work.c:751-754)
+    {
+      int npair = kmax * (kmax - 1) / 2;
+      k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
+      RET(check_launch());
+      k_larft<<<1, 256, sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), P.tau + j, d_st, c.T.as<double>(), kmax);
+      RET(check_launch());
+    }
+    PH(3);
+    // ---- trailing update (dlarfb 'L','T','F','C', src/dgeqrdm_work.c:762-767)
+    {
+      double* W0 = P.A + (size_t)j * lda + j;
+      RET(apply_block_reflector(c, s, W0, lda, W0, lda, mloc, nloc, 1, 1, kmax, d_st));
+    }
+    PH(4);
+    // ---- partial-norm downdate with recompute safeguard (norm_update)
+    {
+      k_norm_downdate<<<ceil_div(nloc, 256), 256, 0, s>>>(P.A, lda, j, n, nrm, nrm_exact, c.list.as<int>(), d_st);
+      RET(check_launch());
+      int blocks = std::min(ceil_div(nloc, 8), 4 * nsm);
+      k_norm_recompute<<<std::max(1, blocks), 256, 0, s>>>(P.A, lda, j, m, c.list.as<int>(), nrm, nrm_exact, d_st);
+      RET(check_launch());
+    }
+    PH(5);
+    RET(read_state(c, s));
+    const BlockState& hs = *c.h_st;
+    if (timing) {
+      for (int q = 0; q < 5; ++q) {
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, c.ph[q], c.ph[q + 1]);
+        ph_ms[q] += ms;
+      }
+    }
+    trail_flops += 4.0 * (double)mloc * (double)(nloc - hs.fjb) * (double)hs.fjb_cmp;
+    if (hs.err & QRDM_EDEV_BARRIER_TIMEOUT) return QRDM_ERR_TIMEOUT;
+    if (hs.err) return QRDM_ERR_INTERNAL;
+    const int fjb_cmp = hs.fjb_cmp;
+    if (fjb_cmp <= 0 || fjb_cmp > hs.fjb) return QRDM_ERR_INTERNAL;
+    P.ncols[it++] = fjb_cmp;
+    recomputes += hs.recompute;
+    maxnrm = bits_to_double(hs.maxnrm_bits);
+    j += fjb_cmp;
+    if (P.stop_mode >= 1 && P.stop_mode <= 3) {
+      if (maxnrm * std::sqrt((double)(nloc - fjb_cmp)) <= eta) break;
+    }
+    if (P.kstop > 0 && j >= P.kstop) break;
+  }
+  CK(cudaEventRecord(c.ev1, s));
+  CK(cudaEventSynchronize(c.ev1));
+  if (stats) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    stats->nblocks = it;
+    stats->recomputes = recomputes;
+    stats->rechecks = 0;
+    stats->columns = j;
+    stats->ms_total = ms;
+    stats->ms_select = ph_ms[0];
+    stats->ms_panel = ph_ms[1];
+    stats->ms_tfactor = ph_ms[2];
+    stats->ms_trail = ph_ms[3];
+    stats->ms_norm = ph_ms[4];
+    stats->trail_flops = trail_flops;
+  }
+#undef PH
+  return 0;
+}
+
+// Argument validation in the order of src/dgeqrdm_work.c:559-589.
+static int validate(int layout, int m, int n, int lda, const double* thres, int nb) {
+  if (layout != QRDM_COL_MAJOR && layout != QRDM_ROW_MAJOR) return -1;
+  if (m <= 0 || n <= 0) return -1;
+  if (lda < std::max(1, m)) return -1;
+  double delta = thres[0], tau_ = thres[1];
+  if (delta < 0.0 || delta > 1.0) return -1;
+  if (tau_ < 0.0 || tau_ > 1.0) return -1;
+  if (nb <= 0) return -1;
+  if (layout != QRDM_COL_MAJOR) return -1;  // documented deviation
+  return 0;
+}
+
+static int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, int* d_jpvt,
+                              double* d_tau, int* ncols, const double* thres, int nb,
+                              const qrdm_options* opt, qrdm_stats* stats) {
+  int v = validate(layout, m, n, lda, thres, nb);
+  if (v) return v;
+  if (nb > QRDM_NB_MAX) return QRDM_ERR_UNSUPPORTED;
+  qrdm_options o;
+  qrdm_default_options(&o);
+  if (opt) o = *opt;
+  DmqrProblem P;
+  P.m = m;
+  P.n = n;
+  P.lda = lda;
+  P.nb = nb;
+  P.A = d_a;
+  P.jpvt = d_jpvt;
+  P.tau = d_tau;
+  P.ncols = ncols;
+  P.delta = thres[0];
+  P.tau_rel = thres[1];
+  P.stop_mode = ncols[0];
+  const double eps = QRDM_EPS64;
+  P.eta = 0.0;
+  if (P.stop_mode == 1) P.eta = eps * n;
+  else if (P.stop_mode == 2) P.eta = eps * std::sqrt((double)n);
+  else if (P.stop_mode == 3) P.eta = thres[2];
+  P.kstop = o.kstop;
+  P.nancheck = o.nancheck;
+  P.precision = o.precision;
+  cudaStream_t s = c.stream();
+  // jpvt: fixed columns are not supported on the device path yet
+  std::vector<int> hj(n);
+  CK(cudaMemcpyAsync(hj.data(), d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int j = 0; j < n; ++j) {
+    if (hj[j] != 0) return QRDM_ERR_UNSUPPORTED;
+    hj[j] = j + 1;
+  }
+  CK(cudaMemcpyAsync(d_jpvt, hj.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  g_launches = 0;
+  int r = dmqr_run(c, P, stats);
+  if (stats) stats->launches = g_launches;
+  return r;
+}
+
+
+// ------------------------------------------- unpivoted QR (LAPACK dgeqrf)
+// Blocked Householder QR with the panel kernel (no early exit) and the
+// block-reflector update; block width 64.
+static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau) {
+  cudaStream_t s = c.stream();
+  const int k = std::min(m, n);
+  const int nbq = 64;
+  CK(c.nrm.ensure(sizeof(double) * 2 * nbq));
+  CK(c.st.ensure(sizeof(BlockState)));
+  CK(c.pan_part.ensure(sizeof(double) * 2 * (size_t)c.nsm * (QRDM_NB_MAX + 1)));
+  CK(c.pan_row.ensure(sizeof(double) * 2 * (QRDM_NB_MAX + 2)));
+  CK(c.pan_bar.ensure(sizeof(unsigned) * 4));
+  CK(c.vtv_part.ensure(sizeof(double) * (size_t)c.nsm * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.T.ensure(sizeof(double) * nbq * nbq));
+  BlockState* d_st = c.st.as<BlockState>();
+  double* nrm = c.nrm.as<double>();
+  for (int j = 0; j < k; j += nbq) {
+    const int kb = std::min(nbq, k - j), mloc = m - j;
+    k_block_init<<<1, 32, 0, s>>>(d_st, kb, 0);
+    k_colnorm_init<<<std::max(1, ceil_div(kb, 8)), 256, 0, s>>>(d_a, lda, j, mloc, j, kb, nrm, nrm + nbq, d_st);
+    RET(check_launch());
+    int G = 1, R = 1;
+    size_t psmem = 0;
+    if (!panel_geometry(c, mloc, kb, &G, &R, &psmem)) return QRDM_ERR_UNSUPPORTED;
+    CK(cudaMemsetAsync(c.pan_bar.p, 0, sizeof(unsigned) * 4, s));
+    PanelArgs pa;
+    pa.A = d_a;
+    pa.lda = lda;
+    pa.j = j;
+    pa.mloc = mloc;
+    pa.tau_rel = 0.0;
+    pa.tau = d_tau + j;
+    pa.nrm = nrm;
+    pa.st = d_st;
+    pa.part = c.pan_part.as<double>();
+    pa.rowbuf = c.pan_row.as<double>();
+    pa.bar = c.pan_bar.as<unsigned>();
+    pa.vtv_part = c.vtv_part.as<double>();
+    pa.rows_per_cta = R;
+    pa.allow_exit = 0;
+    void* args[] = {&pa};
+    CK(cudaLaunchCooperativeKernel((void*)k_panel, dim3(G), dim3(256), args, psmem, s));
+    ++g_launches;
+    int npair = kb * (kb - 1) / 2;
+    k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
+    k_larft<<<1, 256, sizeof(double) * (size_t)kb * kb, s>>>(c.vtv.as<double>(), d_tau + j, d_st, c.T.as<double>(), kb);
+    RET(check_launch());
+    double* W0 = d_a + (size_t)j * lda + j;
+    RET(apply_block_reflector(c, s, W0, lda, W0 + (size_t)kb * lda, lda, mloc, n - j - kb, 0, 1, kb, d_st));
+  }
+  RET(read_state(c, s));
+  if (c.h_st->err & QRDM_EDEV_BARRIER_TIMEOUT) return QRDM_ERR_TIMEOUT;
+  return 0;
+}
+
+// ------------------------------------ C <- Q C  (LAPACK dormqr 'L','N')
+static int dormqr_locked(Ctx& c, int m, int n, int k, const double* d_a, long long lda,
+                         const double* d_tau, double* d_c, long long ldc) {
+  cudaStream_t s = c.stream();
+  const int nbq = 64;
+  CK(c.st.ensure(sizeof(BlockState)));
+  BlockState* d_st = c.st.as<BlockState>();
+  const int last = ((k - 1) / nbq) * nbq;
+  for (int i = last; i >= 0; i -= nbq) {
+    const int ib = std::min(nbq, k - i), mloc = m - i;
+    k_block_init<<<1, 32, 0, s>>>(d_st, ib, ib);
+    RET(check_launch());
+    const double* V = d_a + (size_t)i * lda + i;
+    RET(form_t_stored(c, s, V, lda, mloc, d_tau + i, ib, d_st));
+    RET(apply_block_reflector(c, s, V, lda, d_c + i, ldc, mloc, n, 0, 0, ib, d_st));
+  }
+  RET(read_state(c, s));
+  return 0;
+}
+}  // namespace qrdm
+
+using namespace qrdm;
+
+extern "C" {
+
+void qrdm_default_options(qrdm_options* opt) {
+  memset(opt, 0, sizeof(*opt));
+  opt->precision = QRDM_PREC_FP64;
+  opt->nancheck = 1;
+}
+
+int dgeqrdm_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt, double* d_tau,
+                int* ncols, const double* thres, int nb, const qrdm_options* opt,
+                qrdm_stats* stats) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  return dgeqrdm_dev_locked(*c, matrix_layout, m, n, d_a, lda, d_jpvt, d_tau, ncols, thres, nb, opt, stats);
+}
+
+int dgeqrdm_ex(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau,
+               int* ncols, double* thres, int nb, const qrdm_options* opt, qrdm_stats* stats) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int v = validate(matrix_layout, m, n, lda, thres, nb);
+  if (v) return v;
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  const int minmn = std::min(m, n);
+  CK(c->a.ensure(sizeof(double) * (size_t)m * n));
+  CK(c->jpvt.ensure(sizeof(int) * (size_t)n));
+  CK(c->tau.ensure(sizeof(double) * (size_t)minmn));
+  double* d_a = c->a.as<double>();
+  CK(cudaMemcpy2DAsync(d_a, sizeof(double) * m, a, sizeof(double) * (size_t)lda, sizeof(double) * m, n,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->jpvt.p, jpvt, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->tau.p, tau, sizeof(double) * minmn, cudaMemcpyHostToDevice, s));
+  r = dgeqrdm_dev_locked(*c, matrix_layout, m, n, d_a, m, c->jpvt.as<int>(), c->tau.as<double>(), ncols,
+                         thres, nb, opt, stats);
+  if (r > 0 || r == -1) return r;  // device failure or invalid argument: outputs untouched
+  CK(cudaMemcpy2DAsync(a, sizeof(double) * (size_t)lda, d_a, sizeof(double) * m, sizeof(double) * m, n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(jpvt, c->jpvt.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(tau, c->tau.p, sizeof(double) * minmn, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return r;
+}
+
+int dgeqrdm(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau, int* ncols,
+            double* thres, int nb) {
+  return dgeqrdm_ex(matrix_layout, m, n, a, lda, jpvt, tau, ncols, thres, nb, nullptr, nullptr);
+}
+
+int qrdm_dgeqrf_dev(int matrix_layout, int m, int n, double* d_a, int lda, double* d_tau) {
+  if (matrix_layout != QRDM_COL_MAJOR && matrix_layout != QRDM_ROW_MAJOR) return -1;
+  if (matrix_layout != QRDM_COL_MAJOR) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, m)) return -5;
+  if (m == 0 || n == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  return dgeqrf_locked(*c, m, n, d_a, lda, d_tau);
+}
+
+int qrdm_dgeqrf(int matrix_layout, int m, int n, double* a, int lda, double* tau) {
+  if (matrix_layout != QRDM_COL_MAJOR && matrix_layout != QRDM_ROW_MAJOR) return -1;
+  if (matrix_layout != QRDM_COL_MAJOR) return -1;
+  if (m < 0) return -2;
+  if (n < 0) return -3;
+  if (lda < std::max(1, m)) return -5;
+  if (m == 0 || n == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  const int k = std::min(m, n);
+  CK(c->a.ensure(sizeof(double) * (size_t)m * n));
+  CK(c->tau.ensure(sizeof(double) * (size_t)k));
+  double* d_a = c->a.as<double>();
+  CK(cudaMemcpy2DAsync(d_a, sizeof(double) * m, a, sizeof(double) * (size_t)lda, sizeof(double) * m, n,
+                       cudaMemcpyHostToDevice, s));
+  r = dgeqrf_locked(*c, m, n, d_a, m, c->tau.as<double>());
+  if (r) return r;
+  CK(cudaMemcpy2DAsync(a, sizeof(double) * (size_t)lda, d_a, sizeof(double) * m, sizeof(double) * m, n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(tau, c->tau.p, sizeof(double) * k, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+static int dormqr_check(int layout, int m, int n, int k, int lda, int ldc) {
+  if (layout != QRDM_COL_MAJOR && layout != QRDM_ROW_MAJOR) return -1;
+  if (layout != QRDM_COL_MAJOR) return -1;
+  if (m < 0) return -3;
+  if (n < 0) return -4;
+  if (k < 0 || k > m) return -5;
+  if (lda < std::max(1, m)) return -7;
+  if (ldc < std::max(1, m)) return -10;
+  return 0;
+}
+
+int qrdm_dormqr_dev(int matrix_layout, int m, int n, int k, const double* d_a, int lda,
+                    const double* d_tau, double* d_c, int ldc) {
+  int v = dormqr_check(matrix_layout, m, n, k, lda, ldc);
+  if (v) return v;
+  if (m == 0 || n == 0 || k == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  return dormqr_locked(*c, m, n, k, d_a, lda, d_tau, d_c, ldc);
+}
+
+int qrdm_dormqr(int matrix_layout, int m, int n, int k, const double* a, int lda, const double* tau,
+                double* cm, int ldc) {
+  int v = dormqr_check(matrix_layout, m, n, k, lda, ldc);
+  if (v) return v;
+  if (m == 0 || n == 0 || k == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  CK(c->a.ensure(sizeof(double) * (size_t)m * k + sizeof(double) * (size_t)m * n));
+  CK(c->tau.ensure(sizeof(double) * (size_t)k));
+  double* d_a = c->a.as<double>();
+  double* d_c = d_a + (size_t)m * k;
+  CK(cudaMemcpy2DAsync(d_a, sizeof(double) * m, a, sizeof(double) * (size_t)lda, sizeof(double) * m, k,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpy2DAsync(d_c, sizeof(double) * m, cm, sizeof(double) * (size_t)ldc, sizeof(double) * m, n,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->tau.p, tau, sizeof(double) * k, cudaMemcpyHostToDevice, s));
+  r = dormqr_locked(*c, m, n, k, d_a, m, c->tau.as<double>(), d_c, m);
+  if (r) return r;
+  CK(cudaMemcpy2DAsync(cm, sizeof(double) * (size_t)ldc, d_c, sizeof(double) * m, sizeof(double) * m, n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int qrdm_set_stream(void* stream) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  c->user = (cudaStream_t)stream;
+  c->user_set = stream != nullptr;
+  return 0;
+}
+
+const char* qrdm_version(void) { return "qrdm_gb300 0.1 (sm_103a)"; }
+
+int qrdm_release_workspace(void) {
+  std::lock_guard<std::mutex> lk(g_mu);
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 16) return QRDM_ERR_CUDA;
+  Ctx& c = g_ctx[dev];
+  Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
+                 &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
+                 &c.T, &c.wpart, &c.w2};
+  for (Buf* b : bufs) b->release();
+  return 0;
+}
+
+}  // extern "C"

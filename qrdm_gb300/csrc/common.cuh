@@ -1,0 +1,117 @@
+// common.cuh -- shared device helpers for the DM-QR kernels (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#ifndef QRDM_NB_MAX
+#define QRDM_NB_MAX 128  // largest DM block (nb) the device path accepts
+#endif
+
+// Error words written by kernels (bit flags, OR-ed into BlockState::err).
+enum : int {
+  QRDM_EDEV_BARRIER_TIMEOUT = 1,  // a bounded grid-barrier spin gave up
+  QRDM_EDEV_SMEM = 2,             // a size exceeded a kernel's smem plan
+  QRDM_EDEV_SWAPS = 4,            // swap list overflow
+};
+
+// Per-block control state shared by the kernels of one DM block (device).
+struct BlockState {
+  int nc;          // number of norm candidates (DM_perm :348-351)
+  int fjb;         // columns selected by DM
+  int fjb_cmp;     // columns triangularised by the panel (early exit)
+  int nswap;       // entries of the position permutation
+  int err;         // QRDM_EDEV_* flags
+  int recompute;   // columns whose partial norm was recomputed
+  int rechecks;    // cosines re-evaluated in FP64 (mixed Gram)
+  int nnan;        // NaN entries found by the scan
+  unsigned long long maxnrm_bits;  // max partial norm (bits of a double >= 0)
+  double pad[4];
+};
+
+// ------------------------------------------------------------ reductions
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_max(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmax(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// Non-contracted multiply-add (keeps the rounding of a separate mul + add,
+// the way the reference's C loops round on x86-64).
+__device__ __forceinline__ double mul_add_rn(double a, double b, double c) {
+  return __dadd_rn(__dmul_rn(a, b), c);
+}
+
+// atomic max for non-negative doubles through their bit patterns
+__device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
+  if (!(v > 0.0)) return;
+  atomicMax(addr, (unsigned long long)__double_as_longlong(v));
+}
+
+// --------------------------------------------------- bounded grid barrier
+// Monotonic-counter barrier for cooperative launches: every CTA arrives
+// once per barrier; barrier b completes when the counter reaches
+// nblocks * (b + 1).  The spin is bounded: on timeout the CTA sets
+// QRDM_EDEV_BARRIER_TIMEOUT and returns false so the kernel can unwind.
+#ifndef QRDM_SPIN_LIMIT
+#define QRDM_SPIN_LIMIT (1u << 26)
+#endif
+__device__ __forceinline__ unsigned ld_acquire_u32(const unsigned* p) {
+  unsigned v;
+  asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
+  asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
+  __syncthreads();
+  __shared__ int s_ok;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    red_release_add_u32(counter, 1u);
+    unsigned spins = 0;
+    int ok = 1;
+    while (ld_acquire_u32(counter) < target) {
+      if (++spins > QRDM_SPIN_LIMIT || (*(volatile int*)err & QRDM_EDEV_BARRIER_TIMEOUT)) {
+        atomicOr(err, QRDM_EDEV_BARRIER_TIMEOUT);
+        ok = 0;
+        break;
+      }
+      if (spins > 64) __nanosleep(32);
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// ------------------------------------------------- LAPACK-style scalars
+// Overflow-safe sqrt(x^2 + y^2) following the published dlapy2 algorithm
+// (LAPACK 3.x): w = max(|x|,|y|), z = min(|x|,|y|), w*sqrt(1+(z/w)^2).
+__device__ __forceinline__ double hypot_lapack(double x, double y) {
+  if (x != x) return x;
+  if (y != y) return y;
+  double xa = fabs(x), ya = fabs(y);
+  double w = fmax(xa, ya), z = fmin(xa, ya);
+  if (z == 0.0 || w > 1.7976931348623157e308) return w;
+  double q = z / w;
+  return w * sqrt(1.0 + q * q);
+}
+__device__ __forceinline__ double sign_of(double mag, double s) {
+  double a = fabs(mag);
+  return s >= 0.0 ? a : -a;
+}
+
+// IEEE double constants (binary64): eps = 2^-53 (dlamch('E'), rounding
+// machine epsilon), sfmin = 2^-1022 (dlamch('S')).
+#define QRDM_EPS64 1.1102230246251565e-16
+#define QRDM_SFMIN64 2.2250738585072014e-308
+
+__host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }

@@ -1,0 +1,89 @@
+// kernels.cuh -- kernel declarations and argument blocks shared by the
+// translation units of libqrdm_gb300.
+#pragma once
+#include "common.cuh"
+
+namespace qrdm {
+
+struct Cand {
+  double val;
+  int idx;
+  int pad;
+};
+
+constexpr int kTopkTile = 2048;   // entries sorted per CTA by k_topk_tile
+constexpr int kTopkFinal = 4096;  // entries sorted by k_topk_final
+
+struct PanelArgs {
+  double* A;
+  long long lda;
+  int j;              // window origin A(j, j)
+  int mloc;           // rows of the window (m - j)
+  double tau_rel;     // DM tau_ (early-exit threshold factor)
+  double* tau;        // tau + j
+  const double* nrm;  // partial norms of the window columns (nrm + j)
+  BlockState* st;     // reads fjb, writes fjb_cmp
+  double* part;       // [2][G][NB_MAX+1]
+  double* rowbuf;     // [2][NB_MAX+2]
+  unsigned* bar;      // grid-barrier counter, zero at launch
+  double* vtv_part;   // [G][NB_MAX][NB_MAX]
+  int rows_per_cta;
+  int allow_exit;     // 1: DM early exit (dgeqr2_mia); 0: plain dgeqr2
+};
+
+struct TrailArgs {
+  const double* V;          // reflector block origin (row 0 holds v_0's unit entry)
+  long long ldv;
+  double* C;                // updated matrix, rows aligned with V's rows
+  long long ldc;
+  int mloc;                 // rows of V and C
+  int ncols;                // columns of C counted from C's origin
+  int c_off_from_fjb;       // 1: skip the first st->fjb columns of C (DM-QR)
+  const BlockState* st;     // k = st->fjb_cmp
+  const double* T;
+  int ldt;
+  double* Wpart;            // [nsplit][KT][ldw]
+  double* W2;               // [KT][ldw]
+  int ldw;
+  int rows_per_split;
+  int trans;                // 1: C <- H^T C, 0: C <- H C
+};
+
+// norms.cu
+__global__ void k_colnorm_init(const double* A, long long lda, int row0, int len, int col0,
+                               int ncol, double* nrm, double* nrm_exact, BlockState* st);
+__global__ void k_norm_downdate(const double* A, long long lda, int j, int n, double* nrm,
+                                double* nrm_exact, int* list, BlockState* st);
+__global__ void k_norm_recompute(const double* A, long long lda, int j, int m, const int* list,
+                                 double* nrm, double* nrm_exact, BlockState* st);
+
+// select.cu
+__global__ void k_topk_tile(const double* nrm, const Cand* in_cand, int count, int kmax,
+                            Cand* out);
+__global__ void k_topk_final(const Cand* in_cand, int count, int kmax, double tau_rel, Cand* cand,
+                             BlockState* st);
+void launch_gram_partial(int km, int nchunk, cudaStream_t s, const double* A, long long lda, int j,
+                         int mloc, int rows_per_chunk, const Cand* cand, const BlockState* st,
+                         double* part);
+__global__ void k_gram_reduce(const double* part, int nchunk, int km, const BlockState* st,
+                              double* gram);
+__global__ void k_dm_pick(const Cand* cand, const double* gram, int km, int ncols, int kmax,
+                          double delta, int* jpvt, double* nrm, int2* perm, BlockState* st);
+__global__ void k_permute_columns(double* A, long long lda, int m, int j, const int2* perm,
+                                  const BlockState* st, int max_entries);
+
+// panel.cu
+__global__ void k_block_init(BlockState* st, int fjb, int fjb_cmp);
+__global__ void k_vtv_stored(const double* V, long long ldv, int mloc, int rows_per_chunk,
+                             const BlockState* st, double* vtv_part);
+__global__ void k_panel(PanelArgs p);
+__global__ void k_vtv_reduce(const double* vtv_part, int G, const BlockState* st, double* vtv);
+__global__ void k_larft(const double* vtv, const double* tau, const BlockState* st, double* T,
+                        int ldt);
+
+// trail64.cu
+void launch_trail_w_partial(int KT, dim3 grid, cudaStream_t s, const TrailArgs& a);
+__global__ void k_trail_w_reduce(TrailArgs p, int nsplit, int KT);
+__global__ void k_trail_update(TrailArgs p);
+
+}  // namespace qrdm

@@ -1,0 +1,132 @@
+// norms.cu -- column-norm initialisation and partial-norm downdating.
+//
+// Reference semantics:
+//   norm init      src/dgeqrdm_work.c:672-684   work[j] = dnrm2(A(r0:m, j))
+//   norm_update    src/dgeqrdm_work.c:80-117    dgeqp3-style downdate with the
+//                  recompute safeguard temp2 <= sqrt(eps) -> dnrm2 from scratch
+//
+// K-norm: one warp per column, coalesced 16-byte loads along the column
+// (column-major => contiguous), FP64 sum of squares reduced with warp
+// shuffles.  The sum of squares is accurate when it lies in
+// [2^-960, 2^960]; outside that range (tiny or huge columns) the warp redoes
+// the column with a power-of-two scale, the overflow/underflow-safe route.
+// A NaN in a column makes its sum NaN: the count is returned so the driver
+// can report the reference's NaN error (-13) before factoring.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace qrdm {
+
+__device__ __forceinline__ double column_sumsq(const double* __restrict__ col, int len, int lane) {
+  double s = 0.0;
+  // peel to a 16-byte boundary
+  int head = (int)(((16 - ((uintptr_t)col & 15)) & 15) >> 3);
+  if (head > len) head = len;
+  if (lane < head) s = col[lane] * col[lane];
+  const double2* v = reinterpret_cast<const double2*>(col + head);
+  int nv = (len - head) >> 1;
+  for (int k = lane; k < nv; k += 32) {
+    double2 x = __ldg(v + k);
+    s = fma(x.x, x.x, s);
+    s = fma(x.y, x.y, s);
+  }
+  int tail = head + 2 * nv;
+  if (tail + lane < len) s = fma(col[tail + lane], col[tail + lane], s);
+  return warp_sum(s);
+}
+
+__device__ double column_norm_warp(const double* __restrict__ col, int len, int lane) {
+  double s = column_sumsq(col, len, lane);
+  if (s != s) return s;                          // NaN propagates
+  if (s >= 0x1p-960 && s <= 0x1p960) return sqrt(s);
+  if (s == 0.0) return 0.0;
+  // scaled path: mx = max |x|; norm = mx * sqrt(sum (x/mx)^2)
+  double mx = 0.0;
+  for (int k = lane; k < len; k += 32) mx = fmax(mx, fabs(col[k]));
+  mx = warp_max(mx);
+  if (mx == 0.0 || mx > 1.7976931348623157e308) return mx;
+  int e;
+  frexp(mx, &e);
+  double sc = ldexp(1.0, -e);
+  double t = 0.0;
+  for (int k = lane; k < len; k += 32) {
+    double y = col[k] * sc;
+    t = fma(y, y, t);
+  }
+  t = warp_sum(t);
+  return sqrt(t) * ldexp(1.0, e);
+}
+
+// nrm[c] = nrm_exact[c] = ||A(row0:row0+len, col0+c)||, c < ncol; NaN count.
+__global__ void k_colnorm_init(const double* __restrict__ A, long long lda, int row0, int len,
+                               int col0, int ncol, double* __restrict__ nrm,
+                               double* __restrict__ nrm_exact, BlockState* st) {
+  int warps = blockDim.x >> 5;
+  int lane = threadIdx.x & 31;
+  for (int c = blockIdx.x * warps + (threadIdx.x >> 5); c < ncol; c += gridDim.x * warps) {
+    const double* col = A + (size_t)(col0 + c) * lda + row0;
+    double v = column_norm_warp(col, len, lane);
+    if (lane == 0) {
+      nrm[c] = v;
+      nrm_exact[c] = v;
+      if (v != v) atomicAdd(&st->nnan, 1);
+      else atomic_max_nonneg(&st->maxnrm_bits, v);
+    }
+  }
+}
+
+// Downdate of the partial norms of columns c0..n-1 after the block of fjb_cmp
+// new R rows (rows j..j+fjb_cmp-1).  One thread per column, the squares
+// summed in row order with separately rounded multiply and add, as the
+// reference's loop (src/dgeqrdm_work.c:84-86).  Columns whose estimate fails
+// the safeguard are appended to `list` for a from-scratch recompute.
+__global__ void k_norm_downdate(const double* __restrict__ A, long long lda, int j, int n,
+                                double* __restrict__ nrm, double* __restrict__ nrm_exact,
+                                int* __restrict__ list, BlockState* st) {
+  int fjb_cmp = st->fjb_cmp;
+  int c0 = j + fjb_cmp;
+  int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  double w = nrm[c];
+  if (w == 0.0) return;
+  const double* col = A + (size_t)c * lda + j;
+  double s = 0.0;
+  for (int i = 0; i < fjb_cmp; ++i) s = mul_add_rn(col[i], col[i], s);
+  double t = sqrt(fabs(s)) / w;
+  double d2 = (t + 1.0) * (1.0 - t);
+  t = (0.0 >= d2) ? 0.0 : d2;
+  double r = w / nrm_exact[c];
+  double t2 = t * (r * r);
+  const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53)
+  if (t2 <= tol3z) {
+    int slot = atomicAdd(&st->recompute, 1);
+    list[slot] = c;
+  } else {
+    w *= sqrt(t);
+    nrm[c] = w;
+    atomic_max_nonneg(&st->maxnrm_bits, w);
+  }
+}
+
+// From-scratch partial norms of the listed columns over the rows below the
+// new block of R rows: rows j + fjb_cmp .. m-1 (dnrm2 at src/dgeqrdm_work.c:96).
+__global__ void k_norm_recompute(const double* __restrict__ A, long long lda, int j, int m,
+                                 const int* __restrict__ list, double* __restrict__ nrm,
+                                 double* __restrict__ nrm_exact, BlockState* st) {
+  int count = st->recompute;
+  const int r0 = j + st->fjb_cmp;
+  int warps = blockDim.x >> 5;
+  int lane = threadIdx.x & 31;
+  int len = m - r0;
+  for (int s = blockIdx.x * warps + (threadIdx.x >> 5); s < count; s += gridDim.x * warps) {
+    int c = list[s];
+    double v = len > 0 ? column_norm_warp(A + (size_t)c * lda + r0, len, lane) : 0.0;
+    if (lane == 0) {
+      nrm[c] = v;
+      nrm_exact[c] = v;
+      atomic_max_nonneg(&st->maxnrm_bits, v);
+    }
+  }
+}
+
+}  // namespace qrdm

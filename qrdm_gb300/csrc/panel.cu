@@ -1,0 +1,301 @@
+// panel.cu -- Householder panel with the DM early exit, and its T factor.
+//
+// Reference:
+//   dgeqr2_mia  src/dgeqr2.c:29-195   unblocked QR of the m' x fjb panel;
+//               exits at panel column i > 1 when the sub-diagonal norm falls
+//               below thres = tau_*|R_11| (5e-14 before column 1 sets it)
+//   dlarfg_mia  src/dlarfg.c:28-188   reflector generation + early-exit test
+//   dlarf_      src/dlarf.c:28-211    w = C^T v; C -= tau v w^T
+//   dlarft      called at src/dgeqrdm_work.c:751-754 ('F','C')
+//
+// K-panel (k_panel): cooperative launch, G CTAs (<= one per SM), CTA g owns a
+// slab of R consecutive rows of the panel, held in shared memory for the
+// whole panel.  Each column is scaled by a power of two chosen from its
+// partial norm, which keeps every sum of squares and dot product away from
+// overflow/underflow without changing any rounding (power-of-two scaling is
+// exact); values are unscaled on write-back.
+// Per panel column i, ONE grid barrier: before it each CTA publishes the
+// partial sum of squares of x = A(i+1:, i) and the partial dot products of x
+// with every later panel column; after it every CTA reduces the partials in
+// the same fixed order (bit-identical in all CTAs), forms beta, tau and
+// w_c = C(i,c) + (x.C_c)/(alpha-beta) and applies H(i) to its rows, then
+// computes the partials of column i+1.  At the end each CTA adds its rows'
+// contribution to V^T V (needed by the T factor).
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace qrdm {
+
+struct PanelSmem {
+  double sc[QRDM_NB_MAX];     // per-column scale 2^-e
+  double tw[QRDM_NB_MAX];     // tau * w_c
+  double red[QRDM_NB_MAX + 1];
+  double tau, scal, beta, thres;
+  int exit_flag, tau_zero;
+};
+
+__device__ __forceinline__ double pow2_scale_for(double nrm) {
+  if (!(nrm > 0.0) || !(nrm < 1.7976931348623157e308)) return 1.0;
+  int e;
+  frexp(nrm, &e);
+  return ldexp(1.0, -e);
+}
+
+// Partials for panel column i over this CTA's rows: slot 0 = sum x_r^2,
+// slot s >= 1 = sum x_r * S_{i+s}[r], rows with global index > i.
+__device__ __forceinline__ void panel_partials(const double* __restrict__ S, int R, int nr,
+                                               int grow0, int i, int fjb,
+                                               double* __restrict__ out) {
+  int nslot = fjb - i;
+  int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  int rr0 = i + 1 - grow0;  // first local row strictly below the diagonal
+  if (rr0 < 0) rr0 = 0;
+  const double* x = S + (size_t)i * R;
+  for (int s = wid; s < nslot; s += nw) {
+    const double* y = S + (size_t)(i + s) * R;
+    double acc = 0.0;
+    for (int rr = rr0 + lane; rr < nr; rr += 32) acc = fma(x[rr], y[rr], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) out[s] = acc;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* S = reinterpret_cast<double*>(smem_raw);  // [fjb][R] column-major slab
+  __shared__ PanelSmem sm;
+  const int G = gridDim.x, g = blockIdx.x, R = p.rows_per_cta;
+  const int fjb = p.st->fjb;
+  const int grow0 = g * R;
+  const int nr = max(0, min(R, p.mloc - grow0));
+  const size_t lda = (size_t)p.lda;
+  double* W0 = p.A + (size_t)p.j * lda + p.j;  // window origin A(j, j)
+  const int stride = QRDM_NB_MAX + 1;
+
+  for (int c = threadIdx.x; c < fjb; c += blockDim.x) sm.sc[c] = pow2_scale_for(p.nrm[c]);
+  if (threadIdx.x == 0) {
+    sm.exit_flag = 0;
+    sm.thres = 5e-14;
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < fjb * nr; e += blockDim.x) {
+    int c = e / nr, rr = e % nr;
+    S[(size_t)c * R + rr] = W0[(size_t)c * lda + grow0 + rr] * sm.sc[c];
+  }
+  __syncthreads();
+  panel_partials(S, R, nr, grow0, 0, fjb, p.part + (size_t)g * stride);
+  if (grow0 <= 0 && 0 < grow0 + nr)
+    for (int c = threadIdx.x; c < fjb; c += blockDim.x) p.rowbuf[c] = S[(size_t)c * R + (0 - grow0)];
+
+  int done = fjb;
+  bool ok = true;
+  for (int i = 0; i < fjb; ++i) {
+    const int buf = i & 1;
+    double* part = p.part + (size_t)buf * G * stride;
+    const double* rowb = p.rowbuf + (size_t)buf * (QRDM_NB_MAX + 2);
+    if (!grid_barrier(p.bar, (unsigned)G * (unsigned)(i + 1), &p.st->err)) {
+      ok = false;
+      break;
+    }
+    const int nslot = fjb - i;
+    // fixed-order reduction of the slots over the G CTAs (4 interleaved
+    // accumulators, combined in a fixed order: identical in every CTA)
+    for (int s = threadIdx.x; s < nslot; s += blockDim.x) {
+      double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+      int q = 0;
+      for (; q + 3 < G; q += 4) {
+        a0 += __ldcg(part + (size_t)(q + 0) * stride + s);
+        a1 += __ldcg(part + (size_t)(q + 1) * stride + s);
+        a2 += __ldcg(part + (size_t)(q + 2) * stride + s);
+        a3 += __ldcg(part + (size_t)(q + 3) * stride + s);
+      }
+      for (; q < G; ++q) a0 += __ldcg(part + (size_t)q * stride + s);
+      sm.red[s] = (a0 + a1) + (a2 + a3);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      const double sci = sm.sc[i];
+      const double alpha = __ldcg(rowb + i);
+      const int order = p.mloc - i;  // order of the reflector (dlarfg's n)
+      sm.tau_zero = 1;
+      sm.tau = 0.0;
+      sm.scal = 0.0;
+      sm.beta = alpha;
+      if (order > 1) {
+        double xs = sqrt(sm.red[0]);
+        double xnorm = xs / sci;
+        if (i > 0 && p.allow_exit && xnorm < sm.thres) {
+          sm.exit_flag = 1;
+        } else if (xs != 0.0) {
+          double beta = -sign_of(hypot_lapack(alpha, xs), alpha);
+          sm.tau = (beta - alpha) / beta;
+          sm.scal = 1.0 / (alpha - beta);
+          sm.beta = beta;
+          sm.tau_zero = 0;
+        }
+      }
+      if (!sm.exit_flag) {
+        if (i == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(sm.beta / sci);
+        for (int c = i + 1; c < fjb; ++c) {
+          double w = __ldcg(rowb + c) + sm.scal * sm.red[c - i];
+          sm.tw[c] = sm.tau * w;
+        }
+        if (g == 0) p.tau[i] = sm.tau;
+      }
+    }
+    __syncthreads();
+    if (sm.exit_flag) {
+      done = i;
+      break;
+    }
+    // apply H(i) to this CTA's rows of columns i..fjb-1
+    if (!sm.tau_zero) {
+      const double scal = sm.scal;
+      const int ncol_r = fjb - i - 1;
+      int rr0 = i + 1 - grow0;
+      if (rr0 < 0) rr0 = 0;
+      double* x = S + (size_t)i * R;
+      for (int rr = rr0 + threadIdx.x; rr < nr; rr += blockDim.x) x[rr] *= scal;
+      __syncthreads();
+      for (int e = threadIdx.x; e < ncol_r * nr; e += blockDim.x) {
+        int cc = e / nr, rr = e % nr;
+        int c = i + 1 + cc;
+        int grow = grow0 + rr;
+        if (grow > i) S[(size_t)c * R + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * R + rr]);
+        else if (grow == i) S[(size_t)c * R + rr] -= sm.tw[c];
+      }
+      if (grow0 <= i && i < grow0 + nr && threadIdx.x == 0) x[i - grow0] = sm.beta;
+    }
+    __syncthreads();
+    if (i + 1 < fjb) {
+      double* part_next = p.part + (size_t)(buf ^ 1) * G * stride;
+      panel_partials(S, R, nr, grow0, i + 1, fjb, part_next + (size_t)g * stride);
+      if (grow0 <= i + 1 && i + 1 < grow0 + nr) {
+        double* rb = p.rowbuf + (size_t)(buf ^ 1) * (QRDM_NB_MAX + 2);
+        for (int c = i + 1 + threadIdx.x; c < fjb; c += blockDim.x)
+          rb[c] = S[(size_t)c * R + (i + 1 - grow0)];
+      }
+    }
+  }
+  if (!ok) return;
+  const int kc = done;
+  // write back: V below the diagonal of factored columns is scale-free; all
+  // other entries (R, and the rejected columns) are unscaled.
+  for (int e = threadIdx.x; e < fjb * nr; e += blockDim.x) {
+    int c = e / nr, rr = e % nr;
+    int grow = grow0 + rr;
+    double v = S[(size_t)c * R + rr];
+    if (!(c < kc && grow > c)) v = v / sm.sc[c];
+    W0[(size_t)c * lda + grow] = v;
+  }
+  // partial V^T V over this CTA's rows: vtv[a][b], a < b < kc, with the unit
+  // diagonal of V(:, b) at row b and zeros above it.
+  double* vp = p.vtv_part + (size_t)g * QRDM_NB_MAX * QRDM_NB_MAX;
+  int npair = kc * (kc - 1) / 2;
+  for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+    // decode t -> (a, b), b > a, pairs ordered by b then a
+    int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+    while (b * (b - 1) / 2 > t) --b;
+    while ((b + 1) * b / 2 <= t) ++b;
+    int a = t - b * (b - 1) / 2;
+    const double* va = S + (size_t)a * R;
+    const double* vb = S + (size_t)b * R;
+    double acc = 0.0;
+    int rstart = b - grow0;  // local row of the unit entry of v_b
+    if (rstart < 0) rstart = 0;
+    for (int rr = rstart; rr < nr; ++rr) {
+      int grow = grow0 + rr;
+      double y = (grow == b) ? 1.0 : vb[rr];
+      acc = fma(va[rr], y, acc);
+    }
+    vp[a * QRDM_NB_MAX + b] = acc;
+  }
+  if (g == 0 && threadIdx.x == 0) p.st->fjb_cmp = kc;
+}
+
+// Reset the block record and set the block's column counts (used by the
+// unpivoted QR and the Q application, whose blocks have fixed widths).
+__global__ void k_block_init(BlockState* st, int fjb, int fjb_cmp) {
+  if (threadIdx.x == 0) {
+    BlockState z;
+    memset(&z, 0, sizeof z);
+    z.fjb = fjb;
+    z.fjb_cmp = fjb_cmp;
+    *st = z;
+  }
+}
+
+// V^T V partials of a stored reflector block (rows split in chunks), in the
+// layout k_vtv_reduce sums: part[chunk][a][b], a < b < k = st->fjb_cmp.
+__global__ void __launch_bounds__(256) k_vtv_stored(const double* __restrict__ V, long long ldv,
+                                                    int mloc, int rows_per_chunk,
+                                                    const BlockState* __restrict__ st,
+                                                    double* __restrict__ vtv_part) {
+  const int k = st->fjb_cmp;
+  const int r_begin = blockIdx.x * rows_per_chunk;
+  const int r_end = min(mloc, r_begin + rows_per_chunk);
+  double* vp = vtv_part + (size_t)blockIdx.x * QRDM_NB_MAX * QRDM_NB_MAX;
+  int npair = k * (k - 1) / 2;
+  for (int t = threadIdx.x; t < npair; t += blockDim.x) {
+    int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+    while (b * (b - 1) / 2 > t) --b;
+    while ((b + 1) * b / 2 <= t) ++b;
+    int a = t - b * (b - 1) / 2;
+    double acc = 0.0;
+    for (int r = max(r_begin, b); r < r_end; ++r) {
+      double y = (r == b) ? 1.0 : V[(size_t)b * ldv + r];
+      acc = fma(V[(size_t)a * ldv + r], y, acc);
+    }
+    vp[a * QRDM_NB_MAX + b] = acc;
+  }
+}
+
+// Sum of the V^T V partials over the G panel CTAs (fixed order), packed by
+// column: vtv[b(b-1)/2 + a] for a < b < k.
+__global__ void k_vtv_reduce(const double* __restrict__ vtv_part, int G,
+                             const BlockState* __restrict__ st, double* __restrict__ vtv) {
+  const int k = st->fjb_cmp;
+  int npair = k * (k - 1) / 2;
+  int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npair) return;
+  int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+  while (b * (b - 1) / 2 > t) --b;
+  while ((b + 1) * b / 2 <= t) ++b;
+  int a = t - b * (b - 1) / 2;
+  double s = 0.0;
+  for (int q = 0; q < G; ++q) s += vtv_part[(size_t)q * QRDM_NB_MAX * QRDM_NB_MAX + a * QRDM_NB_MAX + b];
+  vtv[t] = s;
+}
+
+// T factor of the block reflector H(0)..H(k-1) = I - V T V^T ('F','C'):
+// T(i,i) = tau_i; T(0:i, i) = -tau_i T(0:i,0:i) (V(:,0:i)^T v_i) (zero when
+// tau_i = 0), from the reduced V^T V.  One CTA; T is built in shared memory
+// (dynamic, kmax^2 doubles) and stored column-major with leading dim ldt.
+__global__ void __launch_bounds__(256) k_larft(const double* __restrict__ vtv,
+                                               const double* __restrict__ tau,
+                                               const BlockState* __restrict__ st,
+                                               double* __restrict__ T, int ldt) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* sT = reinterpret_cast<double*>(smem_raw);  // [k][k] column-major
+  __shared__ double s_y[QRDM_NB_MAX];
+  const int k = st->fjb_cmp;
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) sT[e] = 0.0;
+  __syncthreads();
+  for (int i = 0; i < k; ++i) {
+    const double ti = tau[i];
+    if (threadIdx.x < i) s_y[threadIdx.x] = -ti * vtv[i * (i - 1) / 2 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < i) {
+      int a = threadIdx.x;
+      double acc = 0.0;
+      if (ti != 0.0)
+        for (int b = a; b < i; ++b) acc = fma(sT[b * k + a], s_y[b], acc);
+      sT[i * k + a] = acc;
+    }
+    if (threadIdx.x == 0) sT[i * k + i] = ti;
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < k * k; e += blockDim.x) T[(size_t)(e / k) * ldt + (e % k)] = sT[e];
+}
+
+}  // namespace qrdm

@@ -1,0 +1,370 @@
+// select.cu -- Deviation-Maximisation block selection on the device.
+//
+// Reference: DM_perm (src/dgeqrdm_work.c:280-418) and permute_marked
+// (src/dgeqrdm_work.c:149-262), called once per DM block (:708-717).
+//
+//   K-topk   k_topk_tile / k_topk_final: the k_max largest partial norms in
+//            the order of the reference's stable sort (norm descending, index
+//            ascending), and the candidate count nc = #{leading entries with
+//            norm > tau_*max}, capped at k_max (:345-351).  Bitonic sorts in
+//            shared memory; only the top k_max survive each tile.
+//   K-gram   k_gram_partial / k_gram_reduce: cosine matrix of the candidate
+//            columns scaled by 1/partial-norm (:365-379), FP64, split over row
+//            chunks, reduced in a fixed order (deterministic).
+//   greedy   k_dm_pick: in norm order take candidate i iff max |cos| with the
+//            taken columns < delta (:382-403), then replay permute_marked's
+//            exchange sequence on a shared-memory bitmap of marks and turn it
+//            into a position permutation (dst <- src).
+//   K-swap   k_permute_columns: applies that permutation to whole columns of
+//            A (all m rows), staged through shared memory, coalesced.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace qrdm {
+
+__device__ __forceinline__ bool cand_before(const Cand& a, const Cand& b) {
+  return a.val > b.val || (a.val == b.val && a.idx < b.idx);
+}
+
+// Bitonic sort of s[0..N) (N power of two) into "before" order.
+template <int N>
+__device__ void bitonic_sort(Cand* s) {
+  for (int k = 2; k <= N; k <<= 1) {
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int t = threadIdx.x; t < N / 2; t += blockDim.x) {
+        int lo = 2 * jj * (t / jj) + (t % jj);
+        int hi = lo + jj;
+        bool up = ((lo & k) == 0);
+        Cand a = s[lo], b = s[hi];
+        bool swap = up ? cand_before(b, a) : cand_before(a, b);
+        if (swap) {
+          s[lo] = b;
+          s[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+constexpr int TOPK_TILE = kTopkTile;
+constexpr int TOPK_FINAL = kTopkFinal;
+
+// Each CTA sorts TOPK_TILE entries and keeps its first kmax.
+// Source: either nrm[col0 + i] (in_cand == nullptr) or in_cand[i].
+__global__ void __launch_bounds__(1024) k_topk_tile(const double* __restrict__ nrm,
+                                                    const Cand* __restrict__ in_cand, int count,
+                                                    int kmax, Cand* __restrict__ out) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cand* s = reinterpret_cast<Cand*>(smem_raw);
+  int base = blockIdx.x * TOPK_TILE;
+  for (int t = threadIdx.x; t < TOPK_TILE; t += blockDim.x) {
+    int i = base + t;
+    Cand c;
+    if (i < count) {
+      if (in_cand) {
+        c = in_cand[i];
+      } else {
+        c.val = nrm[i];
+        c.idx = i;
+      }
+    } else {
+      c.val = -1.0;
+      c.idx = 0x7fffffff;
+    }
+    c.pad = 0;
+    s[t] = c;
+  }
+  __syncthreads();
+  bitonic_sort<TOPK_TILE>(s);
+  for (int t = threadIdx.x; t < kmax; t += blockDim.x) out[blockIdx.x * kmax + t] = s[t];
+}
+
+// Final sort of <= TOPK_FINAL entries; writes the kmax best and nc.
+__global__ void __launch_bounds__(1024) k_topk_final(const Cand* __restrict__ in_cand, int count,
+                                                     int kmax, double tau_rel,
+                                                     Cand* __restrict__ cand, BlockState* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  Cand* s = reinterpret_cast<Cand*>(smem_raw);
+  for (int t = threadIdx.x; t < TOPK_FINAL; t += blockDim.x) {
+    Cand c;
+    if (t < count) {
+      c = in_cand[t];
+    } else {
+      c.val = -1.0;
+      c.idx = 0x7fffffff;
+    }
+    c.pad = 0;
+    s[t] = c;
+  }
+  __syncthreads();
+  bitonic_sort<TOPK_FINAL>(s);
+  for (int t = threadIdx.x; t < kmax; t += blockDim.x) cand[t] = s[t];
+  if (threadIdx.x == 0) {
+    double cut = tau_rel * s[0].val;
+    int nc = 0;
+    while (nc < count && nc < kmax && s[nc].val > cut) ++nc;
+    st->nc = nc;
+  }
+}
+
+// Partial cosine matrix over rows [r_begin, r_end) of the window:
+// part[chunk][p][q] = sum_r as[r][p] * as[r][q], as[r][p] = A(j+r, j+idx_p) * (1/val_p).
+// KM = padded candidate count (64 or 128); 256 threads, each owns a
+// (KM/16) x (KM/16) sub-block of the KM x KM partial.
+template <int KM>
+__global__ void __launch_bounds__(256) k_gram_partial(const double* __restrict__ A, long long lda,
+                                                      int j, int mloc, int rows_per_chunk,
+                                                      const Cand* __restrict__ cand,
+                                                      const BlockState* __restrict__ st,
+                                                      double* __restrict__ part) {
+  constexpr int TR = 16;        // rows per smem stage
+  constexpr int SUB = KM / 16;  // per-thread sub-block edge
+  __shared__ double s_as[TR][KM + 1];
+  __shared__ double s_rc[KM];
+  __shared__ int s_col[KM];
+  int nc = st->nc;
+  if (nc <= 1) return;
+  int r_begin = blockIdx.x * rows_per_chunk;
+  int r_end = min(mloc, r_begin + rows_per_chunk);
+  for (int p = threadIdx.x; p < KM; p += blockDim.x) {
+    if (p < nc) {
+      s_rc[p] = 1.0 / cand[p].val;
+      s_col[p] = j + cand[p].idx;
+    } else {
+      s_rc[p] = 0.0;
+      s_col[p] = -1;
+    }
+  }
+  __syncthreads();
+  int tp = threadIdx.x / 16, tq = threadIdx.x % 16;
+  double acc[SUB][SUB];
+#pragma unroll
+  for (int a = 0; a < SUB; ++a)
+#pragma unroll
+    for (int b = 0; b < SUB; ++b) acc[a][b] = 0.0;
+  for (int r0 = r_begin; r0 < r_end; r0 += TR) {
+    // load TR rows x nc columns (row-fast within a column: coalesced)
+    for (int e = threadIdx.x; e < TR * KM; e += blockDim.x) {
+      int p = e / TR, rr = e % TR;
+      int r = r0 + rr;
+      double v = 0.0;
+      if (p < nc && r < r_end) v = s_rc[p] * A[(size_t)s_col[p] * lda + j + r];
+      s_as[rr][p] = v;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < TR; ++rr) {
+      double x[SUB], y[SUB];
+#pragma unroll
+      for (int a = 0; a < SUB; ++a) x[a] = s_as[rr][tp + 16 * a];
+#pragma unroll
+      for (int b = 0; b < SUB; ++b) y[b] = s_as[rr][tq + 16 * b];
+#pragma unroll
+      for (int a = 0; a < SUB; ++a)
+#pragma unroll
+        for (int b = 0; b < SUB; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+  double* out = part + (size_t)blockIdx.x * KM * KM;
+#pragma unroll
+  for (int a = 0; a < SUB; ++a)
+#pragma unroll
+    for (int b = 0; b < SUB; ++b) out[(tp + 16 * a) * KM + (tq + 16 * b)] = acc[a][b];
+}
+
+// gram[p][q] = sum over chunks (fixed order) of part[chunk][p][q].
+__global__ void k_gram_reduce(const double* __restrict__ part, int nchunk, int km,
+                              const BlockState* __restrict__ st, double* __restrict__ gram) {
+  int nc = st->nc;
+  if (nc <= 1) return;
+  int e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= km * km) return;
+  double s = 0.0;
+  for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * km * km + e];
+  gram[e] = s;
+}
+
+// Greedy pick + permute_marked replay.  One CTA; thread 0 runs the
+// sequential logic on a shared bitmap of marks over the ncols window
+// positions.  Output: perm list (dst, src) of window positions, fjb.
+// Shared memory: bitmap (ncols bits) + swap list + selection arrays.
+__global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
+                                                 const double* __restrict__ gram, int km,
+                                                 int ncols, int kmax, double delta,
+                                                 int* __restrict__ jpvt, double* __restrict__ nrm,
+                                                 int2* __restrict__ perm, BlockState* st) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  // layout: [stage doubles 2*maxsw][stage ints 2*maxsw][sel kmax][pos kmax]
+  //         [swapA maxsw][swapB maxsw][bitmap ceil(ncols/32) words]
+  int maxsw = 2 * kmax + 2;
+  double* s_nv = reinterpret_cast<double*>(smem_raw);
+  int* s_jv = reinterpret_cast<int*>(s_nv + 2 * maxsw);
+  int* s_sel = s_jv + 2 * maxsw;
+  int* s_pos = s_sel + kmax;
+  int* s_swa = s_pos + kmax;
+  int* s_swb = s_swa + maxsw;
+  unsigned* bits = reinterpret_cast<unsigned*>(s_swb + maxsw);
+  __shared__ int s_nsel, s_nswap;
+  int nwords = (ncols + 31) >> 5;
+  for (int w = threadIdx.x; w < nwords; w += blockDim.x) bits[w] = 0u;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int nc = st->nc;
+    int nsel = 1;
+    s_sel[0] = cand[0].idx;
+    s_pos[0] = 0;
+    for (int i = 1; i < nc; ++i) {
+      double worst = 0.0;
+      for (int s = 0; s < nsel; ++s) {
+        double c = fabs(gram[(size_t)s_pos[s] * km + i]);
+        if (worst < c) worst = c;
+      }
+      if (worst < delta && nsel < kmax) {
+        s_pos[nsel] = i;
+        s_sel[nsel] = cand[i].idx;
+        ++nsel;
+      }
+    }
+    for (int s = 0; s < nsel; ++s) bits[s_sel[s] >> 5] |= 1u << (s_sel[s] & 31);
+#define MARK(p) ((bits[(p) >> 5] >> ((p) & 31)) & 1u)
+#define XCHG(p, q)                                                        \
+  do {                                                                    \
+    unsigned bp = MARK(p), bq = MARK(q);                                  \
+    if (bp != bq) {                                                       \
+      bits[(p) >> 5] ^= 1u << ((p) & 31);                                 \
+      bits[(q) >> 5] ^= 1u << ((q) & 31);                                 \
+    }                                                                     \
+    if (nswap < maxsw) {                                                  \
+      s_swa[nswap] = (p);                                                 \
+      s_swb[nswap] = (q);                                                 \
+    }                                                                     \
+    ++nswap;                                                              \
+  } while (0)
+    int nswap = 0;
+    int jb = 0, jt = ncols - 1;
+    for (int s = 0; s < nsel; ++s) {
+      int jc = s_sel[s];
+      while (jb < jt && MARK(jt) == 1u) {
+        XCHG(jt, jb);
+        while (jb < ncols && MARK(jb) == 1u) ++jb;
+      }
+      if (MARK(jc) != 1u) continue;
+      while (jb < ncols && MARK(jb) == 1u) ++jb;
+      if (jc <= jb || jc < nsel) continue;
+      if (MARK(jb) == 0u) {
+        XCHG(jc, jb);
+        ++jb;
+      }
+    }
+#undef XCHG
+#undef MARK
+    if (nswap > maxsw) {
+      atomicOr(&st->err, QRDM_EDEV_SWAPS);
+      nswap = 0;
+    }
+    s_nsel = nsel;
+    s_nswap = nswap;
+  }
+  __syncthreads();
+  int nswap = s_nswap;
+  // Each swap endpoint (first occurrence only) becomes one perm entry whose
+  // source is found by replaying the swaps backwards.
+  int nent = 2 * nswap;
+  int outpos = 0;
+  for (int base = 0; base < nent; base += blockDim.x) {
+    int e = base + threadIdx.x;
+    int keep = 0, dst = -1, src = -1;
+    if (e < nent) {
+      int s = e >> 1;
+      dst = (e & 1) ? s_swb[s] : s_swa[s];
+      keep = 1;
+      for (int t = 0; t < s && keep; ++t)
+        if (s_swa[t] == dst || s_swb[t] == dst) keep = 0;
+      if (keep && (e & 1) && s_swa[s] == dst) keep = 0;
+      if (keep) {
+        int x = dst;
+        for (int t = nswap - 1; t >= 0; --t) {
+          if (x == s_swa[t]) x = s_swb[t];
+          else if (x == s_swb[t]) x = s_swa[t];
+        }
+        src = x;
+        if (src == dst) keep = 0;
+      }
+    }
+    // compact with a block-wide ballot scan
+    unsigned ball = __ballot_sync(0xffffffffu, keep);
+    __shared__ int s_wcount[8];
+    int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) s_wcount[wid] = __popc(ball);
+    __syncthreads();
+    int off = outpos;
+    for (int w = 0; w < wid; ++w) off += s_wcount[w];
+    off += __popc(ball & ((1u << lane) - 1u));
+    if (keep) perm[off] = make_int2(dst, src);
+    int total = 0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) total += s_wcount[w];
+    outpos += total;
+    __syncthreads();
+  }
+  __syncthreads();
+  // permute jpvt and the partial norms (not the "exact" norms: the reference
+  // swaps work[] but not work[n+...], src/dgeqrdm_work.c:410-415 with :172-174).
+  // All sources are staged before any destination is written.
+  int np = outpos;
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    int2 pe = perm[e];
+    s_jv[e] = jpvt[pe.y];
+    s_nv[e] = nrm[pe.y];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < np; e += blockDim.x) {
+    int2 pe = perm[e];
+    jpvt[pe.x] = s_jv[e];
+    nrm[pe.x] = s_nv[e];
+  }
+  if (threadIdx.x == 0) {
+    st->fjb = s_nsel;
+    st->nswap = np;
+  }
+}
+
+// Whole-column permutation of the window: column (j + dst) <- column (j + src)
+// for every perm entry, all m rows.  CTA = ROWS rows; each entry's rows are
+// staged in shared memory first, so entries may form cycles.
+__global__ void __launch_bounds__(256) k_permute_columns(double* __restrict__ A, long long lda,
+                                                         int m, int j,
+                                                         const int2* __restrict__ perm,
+                                                         const BlockState* __restrict__ st,
+                                                         int max_entries) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  constexpr int ROWS = 32;
+  double* s = reinterpret_cast<double*>(smem_raw);  // [max_entries][ROWS]
+  int np = st->nswap;
+  if (np <= 0) return;
+  if (np > max_entries) np = max_entries;
+  int r0 = blockIdx.x * ROWS;
+  for (int e = threadIdx.x; e < np * ROWS; e += blockDim.x) {
+    int t = e / ROWS, rr = e % ROWS;
+    int r = r0 + rr;
+    if (r < m) s[t * ROWS + rr] = A[(size_t)(j + perm[t].y) * lda + r];
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < np * ROWS; e += blockDim.x) {
+    int t = e / ROWS, rr = e % ROWS;
+    int r = r0 + rr;
+    if (r < m) A[(size_t)(j + perm[t].x) * lda + r] = s[t * ROWS + rr];
+  }
+}
+
+void launch_gram_partial(int km, int nchunk, cudaStream_t s, const double* A, long long lda, int j,
+                         int mloc, int rows_per_chunk, const Cand* cand, const BlockState* st,
+                         double* part) {
+  if (km == 64)
+    k_gram_partial<64><<<nchunk, 256, 0, s>>>(A, lda, j, mloc, rows_per_chunk, cand, st, part);
+  else
+    k_gram_partial<128><<<nchunk, 256, 0, s>>>(A, lda, j, mloc, rows_per_chunk, cand, st, part);
+}
+
+}  // namespace qrdm

@@ -1,0 +1,153 @@
+"""GPU DM-QR (libqrdm_gb300, FP64 path) against the reference's known answers.
+
+Parity bar (mdessole/qrdm has no tests of its own; the golden fixtures were
+produced by the compiled reference, see tests/golden/make_golden.py):
+  * info identical;
+  * jpvt and the DM block sizes (ncols) identical over the gap-separated
+    prefix: the leading DM blocks in which every data-dependent decision of
+    the oracle's run (bit-identical to the reference) is at least GAP noise
+    units from its threshold, one unit being max(m,n) * eps * ||A||_F (the
+    backward-error scale; see oracle/dmqr_oracle.c).  Past the first block
+    with a smaller margin, any backward-stable implementation may pick
+    differently (calibrated by perturbing the input by 100 eps ||A||);
+  * the leading R block of the separated prefix within
+    RTOL_R * n * eps * ||A||_F of the reference's (Frobenius);
+  * backward error ||A P - Q R||_F / ||A||_F <= 10 max(m,n) eps and
+    ||I - Q^T Q||_F <= 100 max(m,n) eps in every case.
+"""
+import numpy as np
+import pytest
+
+from conftest import load_golden
+
+EPS = 2.0 ** -53
+GAP = 100.0
+RTOL_R = 64.0
+
+GOLDEN_NAMES = list(load_golden().keys())
+
+
+def run_gpu(A0, p, **kw):
+    import qrdm_gb300
+
+    delta, tau_, nb, stop, eta = p
+    return qrdm_gb300.dgeqrdm(A0, nb=int(nb), delta=delta, tau_=tau_, stop=int(stop),
+                              eta=eta, **kw)
+
+
+def separated(oracle, A0, p):
+    """Oracle run with margins -> (blocks, columns) of the separated prefix."""
+    from oracle.oracle import run_dmqr, separated_prefix
+
+    delta, tau_, nb, stop, eta = p
+    r = run_dmqr(oracle, A0, delta=delta, tau_=tau_, nb=int(nb), stop=int(stop), eta=eta,
+                 margins=True)
+    return separated_prefix(r, GAP), r
+
+
+def check_against(A0, gpu, ref, prefix, label: str):
+    """prefix = (blocks, columns) that must agree exactly."""
+    from qrdm_gb300.metrics import factor_metrics
+
+    m, n = A0.shape
+    assert gpu["info"] == ref["info"], (label, gpu["info"], ref["info"])
+    if gpu["info"] != 0:
+        return
+    nb_sep, cols = prefix
+    assert np.array_equal(gpu["ncols"][:nb_sep], ref["ncols"][:nb_sep]), (
+        label, gpu["ncols"][:nb_sep], ref["ncols"][:nb_sep])
+    assert np.array_equal(gpu["jpvt"][:cols], ref["jpvt"][:cols]), (label, "jpvt prefix", cols)
+    if nb_sep == int(np.count_nonzero(ref["ncols"])):
+        assert np.array_equal(gpu["ncols"], ref["ncols"]), label
+        assert np.array_equal(gpu["jpvt"], ref["jpvt"]), label
+    if cols > 0:
+        an = np.linalg.norm(A0)
+        dR = np.linalg.norm(np.triu(gpu["A"][:cols, :cols]) - np.triu(ref["A"][:cols, :cols]))
+        assert dR <= RTOL_R * n * EPS * max(an, 1e-300), (label, dR / max(an, 1e-300))
+    k = int(np.sum(gpu["ncols"][:int(np.count_nonzero(gpu["ncols"]))]))
+    met = factor_metrics(A0, gpu["A"], gpu["tau"], gpu["jpvt"], k=min(k, min(m, n)))
+    bound = 10 * max(m, n) * EPS
+    # the rejected-but-untriangularised part of a stopped factorisation is
+    # still exact: A P = Q [R11 R12; 0 R22]
+    assert met["backward"] <= bound, (label, met["backward"])
+    assert met["orth"] <= bound * 10, (label, met["orth"])
+    return met
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_golden_case(gpu_lib, golden, oracle, name):
+    c = golden[name]
+    A0 = np.asfortranarray(c["A_in"])
+    p = tuple(c["params"].tolist())
+    prefix, _ = separated(oracle, A0, p)
+    gpu = run_gpu(A0, p)
+    ref = {"A": c["A_out"], "jpvt": c["jpvt"], "tau": c["tau"], "ncols": c["ncols"],
+           "info": int(c["info"][0])}
+    check_against(A0, gpu, ref, prefix, label=name)
+
+
+@pytest.mark.gpu
+def test_config1_graded_1000(gpu_lib, oracle):
+    """DM-QR CPU-parity workload: 1000 x 1000, s_i = 10^(-12 (i-1)/999)."""
+    from oracle.oracle import run_dmqr
+    from qrdm_gb300 import workloads as W
+
+    A0 = W.graded_svd(1000, seed=0)
+    prefix, ref = separated(oracle, A0, (0.9, 0.15, 64, 0, 0.0))
+    assert prefix[0] >= 5, prefix
+    gpu = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
+    check_against(A0, gpu, ref, prefix, label="config1")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kind", ["gaussian", "kahan"])
+def test_config2_4096(gpu_lib, oracle, kind):
+    """Plain FP64 DM-QR on 4096 x 4096: i.i.d. N(0,1) and the perturbed Kahan
+    matrix (pivot ties, norm downdating)."""
+    from qrdm_gb300 import workloads as W
+
+    A0 = W.gaussian(4096, 4096, seed=1) if kind == "gaussian" else W.kahan(4096, seed=2)
+    prefix, ref = separated(oracle, A0, (0.9, 0.15, 64, 0, 0.0))
+    gpu = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
+    check_against(A0, gpu, ref, prefix, label=f"config2-{kind}")
+
+
+@pytest.mark.gpu
+def test_nan_input_reports_minus_13(gpu_lib):
+    from qrdm_gb300 import workloads as W
+
+    A0 = W.gaussian(40, 30, seed=3)
+    A0[7, 11] = np.nan
+    r = run_gpu(A0, (0.9, 0.15, 16, 0, 0.0))
+    assert r["info"] == -13
+
+
+@pytest.mark.gpu
+def test_invalid_arguments(gpu_lib):
+    from qrdm_gb300 import QRDM
+
+    A = np.asfortranarray(np.random.default_rng(0).standard_normal((8, 6)))
+    jp = np.zeros(6, np.int32)
+    tau = np.zeros(6)
+    nc = np.zeros(6, np.int32)
+    good = np.array([0.9, 0.15])
+    assert QRDM.QRDM(103, 8, 6, A, 8, jp, tau, nc, good, 4) == -1   # layout
+    assert QRDM.QRDM(102, 8, 6, A, 7, jp, tau, nc, good, 4) == -1   # lda < m
+    assert QRDM.QRDM(102, 8, 6, A, 8, jp, tau, nc, np.array([1.5, 0.1]), 4) == -1
+    assert QRDM.QRDM(102, 8, 6, A, 8, jp, tau, nc, np.array([0.5, -0.1]), 4) == -1
+    assert QRDM.QRDM(102, 8, 6, A, 8, jp, tau, nc, good, 0) == -1   # nb
+    assert QRDM.QRDM(101, 8, 6, A, 8, jp, tau, nc, good, 4) == -1   # row-major rejected
+
+
+@pytest.mark.gpu
+def test_repeatable_bits(gpu_lib):
+    """Two runs on the same input give bit-identical results (fixed-order
+    reductions everywhere)."""
+    from qrdm_gb300 import workloads as W
+
+    A0 = W.gaussian(700, 500, seed=9)
+    a = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
+    b = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
+    assert np.array_equal(a["A"], b["A"]) and np.array_equal(a["tau"], b["tau"])
+    assert np.array_equal(a["jpvt"], b["jpvt"])
