@@ -55,6 +55,7 @@ struct Ctx {
   Buf a, jpvt, tau;                        // device copies for host entry points
   Buf nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st;
   Buf pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
+  Buf qF, qg, qpart, qst;
   BlockState* h_st = nullptr;              // pinned host copy of the block record
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ph[8] = {};
@@ -100,6 +101,7 @@ static int ctx_get(Ctx** out) {
     CK(cudaFuncSetAttribute(k_permute_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_larft, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 2048));
     CK(cudaFuncSetAttribute(k_trail_w_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
+    CK(cudaFuncSetAttribute(k_qp3_gemv, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536));
     g_attr_done[dev] = true;
   }
   *out = &c;
@@ -127,6 +129,7 @@ struct DmqrProblem {
   int* ncols;    // host
   double delta, tau_rel, eta;
   int stop_mode, kstop, nancheck, precision;
+  int nfxd = 0;  // fixed leading columns already factored
 };
 
 #define RET(x)                 \
@@ -215,6 +218,9 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
   return 0;
 }
 
+static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
+                         std::vector<int>& hj, int* err);
+
 static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   cudaStream_t s = c.stream();
   const bool timing = stats && stats->timing;
@@ -260,7 +266,8 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
 
   CK(cudaEventRecord(c.ev0, s));
   // ---- norm init (src/dgeqrdm_work.c:672-684) + NaN detection
-  const int nfxd = 0;
+  const int nfxd = P.nfxd;
+  if (nfxd >= minmn) return 0;
   CK(cudaMemsetAsync(d_st, 0, sizeof(BlockState), s));
   {
     int ncol = n - nfxd;
@@ -465,16 +472,14 @@ static int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int
   P.nancheck = o.nancheck;
   P.precision = o.precision;
   cudaStream_t s = c.stream();
-  // jpvt: fixed columns are not supported on the device path yet
   std::vector<int> hj(n);
   CK(cudaMemcpyAsync(hj.data(), d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
-  for (int j = 0; j < n; ++j) {
-    if (hj[j] != 0) return QRDM_ERR_UNSUPPORTED;
-    hj[j] = j + 1;
-  }
-  CK(cudaMemcpyAsync(d_jpvt, hj.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   g_launches = 0;
+  int err = 0;
+  P.nfxd = fixed_columns(c, m, n, d_a, lda, d_tau, hj, &err);
+  if (err) return err;
+  CK(cudaMemcpyAsync(d_jpvt, hj.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   int r = dmqr_run(c, P, stats);
   if (stats) stats->launches = g_launches;
   return r;
@@ -539,19 +544,163 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
 
 // ------------------------------------ C <- Q C  (LAPACK dormqr 'L','N')
 static int dormqr_locked(Ctx& c, int m, int n, int k, const double* d_a, long long lda,
-                         const double* d_tau, double* d_c, long long ldc) {
+                         const double* d_tau, double* d_c, long long ldc, int trans = 0) {
   cudaStream_t s = c.stream();
   const int nbq = 64;
   CK(c.st.ensure(sizeof(BlockState)));
   BlockState* d_st = c.st.as<BlockState>();
   const int last = ((k - 1) / nbq) * nbq;
-  for (int i = last; i >= 0; i -= nbq) {
+  // Q C = H(1)(H(2)(...H(k) C)): blocks last to first;  Q^T C: first to last
+  for (int t = 0; t <= last / nbq; ++t) {
+    const int i = trans ? t * nbq : last - t * nbq;
     const int ib = std::min(nbq, k - i), mloc = m - i;
     k_block_init<<<1, 32, 0, s>>>(d_st, ib, ib);
     RET(check_launch());
     const double* V = d_a + (size_t)i * lda + i;
     RET(form_t_stored(c, s, V, lda, mloc, d_tau + i, ib, d_st));
-    RET(apply_block_reflector(c, s, V, lda, d_c + i, ldc, mloc, n, 0, 0, ib, d_st));
+    RET(apply_block_reflector(c, s, V, lda, d_c + i, ldc, mloc, n, 0, trans, ib, d_st));
+  }
+  RET(read_state(c, s));
+  return 0;
+}
+
+// Fixed leading columns (jpvt[j] != 0) of dgeqrdm/dgeqp3
+// (src/dgeqrdm_work.c:594-635, LAPACK dgeqp3): moved to the front by
+// column exchanges (jpvt updated on the host copy hj), factored without
+// pivoting, Q^T applied to the remaining columns.  Returns nfxd (>= 0) or
+// a negative/positive error code via *err.
+static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
+                         std::vector<int>& hj, int* err) {
+  cudaStream_t s = c.stream();
+  int nfxd = 0;
+  *err = 0;
+  for (int j = 0; j < n; ++j) {
+    if (hj[j] != 0) {
+      if (j != nfxd) {
+        k_swap_columns<<<ceil_div(m, 256), 256, 0, s>>>(d_a, lda, m, j, nfxd);
+        if ((*err = check_launch())) return 0;
+        hj[j] = hj[nfxd];
+        hj[nfxd] = j + 1;
+      } else {
+        hj[j] = j + 1;
+      }
+      ++nfxd;
+    } else {
+      hj[j] = j + 1;
+    }
+  }
+  if (nfxd > 0) {
+    const int na = std::min(m, nfxd);
+    if ((*err = dgeqrf_locked(c, m, na, d_a, lda, d_tau))) return 0;
+    if (na < n) {
+      if ((*err = dormqr_locked(c, m, n - na, na, d_a, lda, d_tau, d_a + (size_t)na * lda, lda, 1)))
+        return 0;
+    }
+  }
+  return nfxd;
+}
+
+// ------------------------------------------------------------ QP3 blocks
+// One dlaqps block (qp2 = 0) or one dlaqp2 step (jb = 1, qp2 = 1) at column
+// j; returns the number of columns factored via *kb (blocked case reads it
+// back from the device; the dlaqp2 step always factors one).
+static int qp3_block(Ctx& c, cudaStream_t s, int m, int n, double* d_a, long long lda,
+                     int* d_jpvt, double* d_tau, double* vn1, double* vn2, int j, int jb, int qp2,
+                     int* list, bool readback, int* kb) {
+  Qp3State* st = reinterpret_cast<Qp3State*>(c.qst.p);
+  const int nw = n - j;
+  double* W = d_a + (size_t)j * lda;
+  double* F = c.qF.as<double>();
+  const long long ldf = n;
+  k_qp3_reset<<<1, 32, 0, s>>>(st);
+  RET(check_launch());
+  const int nparts = ceil_div(m, 256);
+  const int lastrk = std::min(m, nw + j);  // 1-based LASTRK of dlaqps
+  for (int k = 0; k < jb; ++k) {
+    const int rk = j + k;
+    k_qp3_pivot<<<1, 1024, 0, s>>>(k, nw, vn1 + j, vn2 + j, d_jpvt + j, F, ldf, st);
+    RET(check_launch());
+    k_qp3_column<<<nparts, 256, 0, s>>>(W, lda, m, k, rk, F, ldf, c.qpart.as<double>(), st);
+    RET(check_launch());
+    k_qp3_house<<<1, 256, 0, s>>>(m, rk, c.qpart.as<double>(), nparts, d_tau + rk, st);
+    RET(check_launch());
+    const int mrem = m - rk;
+    const int tiles = ceil_div(nw, 64);
+    int nsplit = std::max(1, std::min(ceil_div(2 * c.nsm, tiles), ceil_div(mrem, 256)));
+    int rps = ceil_div(mrem, nsplit);
+    if (rps > 8192) {
+      nsplit = ceil_div(mrem, 8192);
+      rps = ceil_div(mrem, nsplit);
+    }
+    CK(c.qg.ensure(sizeof(double) * (size_t)nsplit * n));
+    k_qp3_gemv<<<dim3(tiles, nsplit), 256, sizeof(double) * (size_t)rps, s>>>(
+        W, lda, m, nw, k, rk, rps, c.qg.as<double>(), n, st);
+    RET(check_launch());
+    const int lastrk_ok = qp2 ? 1 : ((rk + 1) < lastrk);
+    k_qp3_fupdate<<<ceil_div(nw, 256), 256, 0, s>>>(W, lda, m, nw, k, rk, lastrk_ok, c.qg.as<double>(),
+                                                     nsplit, n, F, ldf, vn1 + j, vn2 + j, list, qp2, st);
+    RET(check_launch());
+  }
+  k_qp3_gemm<<<dim3(std::max(1, ceil_div(nw, 64)), std::max(1, ceil_div(m - j, 64))), 256, 0, s>>>(
+      W, lda, m, nw, j, F, ldf, st);
+  RET(check_launch());
+  k_qp3_recompute<<<std::max(1, std::min(ceil_div(nw, 8), 2 * c.nsm)), 256, 0, s>>>(
+      W, lda, m, j, list, vn1 + j, vn2 + j, st);
+  RET(check_launch());
+  if (readback) {
+    int hkb = 0;
+    CK(cudaMemcpyAsync(&hkb, &reinterpret_cast<int*>(st)[2], sizeof(int), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    *kb = hkb;
+  } else {
+    *kb = jb;
+  }
+  return 0;
+}
+
+static int dgeqp3_locked(Ctx& c, int m, int n, double* d_a, long long lda, int* d_jpvt,
+                         double* d_tau) {
+  cudaStream_t s = c.stream();
+  const int minmn = std::min(m, n);
+  std::vector<int> hj(n);
+  CK(cudaMemcpyAsync(hj.data(), d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  g_launches = 0;
+  int err = 0;
+  const int nfxd = fixed_columns(c, m, n, d_a, lda, d_tau, hj, &err);
+  if (err) return err;
+  CK(cudaMemcpyAsync(d_jpvt, hj.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  if (nfxd >= minmn) return read_state(c, s);
+  const int nbq = 32, nx = 128;  // LAPACK ilaenv: NB(DGEQRF) = 32, NX = 128
+  CK(c.nrm.ensure(sizeof(double) * 2 * (size_t)n));
+  CK(c.list.ensure(sizeof(int) * (size_t)n));
+  CK(c.st.ensure(sizeof(BlockState)));
+  CK(c.qF.ensure(sizeof(double) * (size_t)n * nbq));
+  CK(c.qpart.ensure(sizeof(double) * (size_t)ceil_div(m, 256)));
+  CK(c.qst.ensure(qp3_state_bytes()));
+  double* vn1 = c.nrm.as<double>();
+  double* vn2 = vn1 + n;
+  CK(cudaMemsetAsync(c.st.p, 0, sizeof(BlockState), s));
+  k_colnorm_init<<<std::max(1, std::min(ceil_div(n - nfxd, 8), 8 * c.nsm)), 256, 0, s>>>(
+      d_a, lda, nfxd, m - nfxd, nfxd, n - nfxd, vn1 + nfxd, vn2 + nfxd, c.st.as<BlockState>());
+  RET(check_launch());
+  const int sminmn = minmn - nfxd;
+  int j = nfxd;
+  if (nbq < sminmn && nx < sminmn) {
+    const int topbmn = minmn - nx;  // 0-based: blocked while j < topbmn
+    while (j < topbmn) {
+      const int jb = std::min(nbq, topbmn - j);
+      int kb = 0;
+      RET(qp3_block(c, s, m, n, d_a, lda, d_jpvt, d_tau, vn1, vn2, j, jb, 0, c.list.as<int>(), true, &kb));
+      if (kb <= 0) return QRDM_ERR_INTERNAL;
+      j += kb;
+    }
+  }
+  // dlaqp2 on the rest, one column at a time
+  while (j < minmn) {
+    int kb = 0;
+    RET(qp3_block(c, s, m, n, d_a, lda, d_jpvt, d_tau, vn1, vn2, j, 1, 1, c.list.as<int>(), false, &kb));
+    j += 1;
   }
   RET(read_state(c, s));
   return 0;
@@ -703,6 +852,53 @@ int qrdm_dormqr(int matrix_layout, int m, int n, int k, const double* a, int lda
   return 0;
 }
 
+static int dgeqp3_check(int layout, int m, int n, int lda) {
+  if (layout != QRDM_COL_MAJOR && layout != QRDM_ROW_MAJOR) return -1;
+  if (layout != QRDM_COL_MAJOR) return -1;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, m)) return -4;
+  return 0;
+}
+
+int dgeqp3_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt, double* d_tau) {
+  int v = dgeqp3_check(matrix_layout, m, n, lda);
+  if (v) return v;
+  if (m == 0 || n == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  return dgeqp3_locked(*c, m, n, d_a, lda, d_jpvt, d_tau);
+}
+
+int dgeqp3(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau) {
+  int v = dgeqp3_check(matrix_layout, m, n, lda);
+  if (v) return v;
+  if (m == 0 || n == 0) return 0;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  const int minmn = std::min(m, n);
+  CK(c->a.ensure(sizeof(double) * (size_t)m * n));
+  CK(c->jpvt.ensure(sizeof(int) * (size_t)n));
+  CK(c->tau.ensure(sizeof(double) * (size_t)minmn));
+  double* d_a = c->a.as<double>();
+  CK(cudaMemcpy2DAsync(d_a, sizeof(double) * m, a, sizeof(double) * (size_t)lda, sizeof(double) * m, n,
+                       cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(c->jpvt.p, jpvt, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  r = dgeqp3_locked(*c, m, n, d_a, m, c->jpvt.as<int>(), c->tau.as<double>());
+  if (r) return r;
+  CK(cudaMemcpy2DAsync(a, sizeof(double) * (size_t)lda, d_a, sizeof(double) * m, sizeof(double) * m, n,
+                       cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(jpvt, c->jpvt.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(tau, c->tau.p, sizeof(double) * minmn, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
 int qrdm_set_stream(void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx* c = nullptr;
@@ -722,7 +918,7 @@ int qrdm_release_workspace(void) {
   Ctx& c = g_ctx[dev];
   Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
                  &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
-                 &c.T, &c.wpart, &c.w2};
+                 &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst};
   for (Buf* b : bufs) b->release();
   return 0;
 }

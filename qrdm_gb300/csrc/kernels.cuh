@@ -86,4 +86,26 @@ void launch_trail_w_partial(int KT, dim3 grid, cudaStream_t s, const TrailArgs& 
 __global__ void k_trail_w_reduce(TrailArgs p, int nsplit, int KT);
 __global__ void k_trail_update(TrailArgs p);
 
+// qp3.cu
+struct Qp3State;
+size_t qp3_state_bytes();
+__global__ void k_qp3_reset(Qp3State* st);
+__global__ void k_qp3_pivot(int k, int nw, double* vn1, double* vn2, int* jpvt, double* F,
+                            long long ldf, Qp3State* st);
+__global__ void k_qp3_column(double* W, long long lda, int m, int k, int rk, const double* F,
+                             long long ldf, double* part, Qp3State* st);
+__global__ void k_qp3_house(int m, int rk, const double* part, int nparts, double* tau,
+                            Qp3State* st);
+__global__ void k_qp3_gemv(const double* W, long long lda, int m, int nw, int k, int rk,
+                           int rows_per_split, double* g, long long ldg, const Qp3State* st);
+__global__ void k_qp3_fupdate(double* W, long long lda, int m, int nw, int k, int rk,
+                              int lastrk_ok, const double* g, int nsplit, long long ldg, double* F,
+                              long long ldf, double* vn1, double* vn2, int* list, int qp2,
+                              Qp3State* st);
+__global__ void k_qp3_gemm(double* W, long long lda, int m, int nw, int rk0, const double* F,
+                           long long ldf, const Qp3State* st);
+__global__ void k_qp3_recompute(const double* W, long long lda, int m, int rk0, const int* list,
+                                double* vn1, double* vn2, const Qp3State* st);
+__global__ void k_swap_columns(double* A, long long lda, int m, int p, int q);
+
 }  // namespace qrdm
