@@ -14,55 +14,12 @@
 #include <mutex>
 #include <vector>
 
-#include "../../include/qrdm_gb300.h"
-#include "common.cuh"
-#include "kernels.cuh"
+#include "driver.h"
 
 namespace qrdm {
 
-// ------------------------------------------------------------ workspace
-struct Buf {
-  void* p = nullptr;
-  size_t cap = 0;
-  cudaError_t ensure(size_t bytes) {
-    if (bytes <= cap) return cudaSuccess;
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-    size_t b = std::max<size_t>(bytes, 256);
-    cudaError_t e = cudaMalloc(&p, b);
-    if (e == cudaSuccess) cap = b;
-    return e;
-  }
-  void release() {
-    if (p) cudaFree(p);
-    p = nullptr;
-    cap = 0;
-  }
-  template <class T>
-  T* as() const {
-    return reinterpret_cast<T*>(p);
-  }
-};
-
-struct Ctx {
-  int dev = -1;
-  int nsm = 0;
-  size_t smem_optin = 0;
-  cudaStream_t own = nullptr;
-  cudaStream_t user = nullptr;
-  bool user_set = false;
-  Buf a, jpvt, tau;                        // device copies for host entry points
-  Buf nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st;
-  Buf pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
-  Buf qF, qg, qpart, qst;
-  BlockState* h_st = nullptr;              // pinned host copy of the block record
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  cudaEvent_t ph[8] = {};
-  cudaStream_t stream() const { return user_set ? user : own; }
-};
-
 static std::mutex g_mu;
+std::mutex& library_lock() { return g_mu; }
 static Ctx g_ctx[16];
 static bool g_attr_done[16];
 
@@ -93,7 +50,16 @@ static int ctx_get(Ctx** out) {
     for (auto& e : c.ph) CK(cudaEventCreate(&e));
   }
   if (!g_attr_done[dev]) {
-    int big = (int)c.smem_optin;
+    int r = set_kernel_attributes((int)c.smem_optin);
+    if (r) return r;
+    g_attr_done[dev] = true;
+  }
+  *out = &c;
+  return 0;
+}
+
+int set_kernel_attributes(int big) {
+  {
     CK(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
     CK(cudaFuncSetAttribute(k_topk_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkTile * (int)sizeof(Cand)));
     CK(cudaFuncSetAttribute(k_topk_final, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkFinal * (int)sizeof(Cand)));
@@ -102,9 +68,7 @@ static int ctx_get(Ctx** out) {
     CK(cudaFuncSetAttribute(k_larft, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 2048));
     CK(cudaFuncSetAttribute(k_trail_w_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_qp3_gemv, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536));
-    g_attr_done[dev] = true;
   }
-  *out = &c;
   return 0;
 }
 
@@ -150,9 +114,58 @@ static double bits_to_double(unsigned long long b) {
   return d;
 }
 
+// Upper bound of the Gram row chunks (see the DM candidates step).
+static int gram_chunks_max(int m, int nsm) { return std::max(1, std::min(2 * nsm, ceil_div(m, 32))); }
+// Panel CTAs for a window of mloc rows (one per SM at most, >= 64 rows each).
+static int panel_ctas(int mloc, int nsm) { return std::max(1, std::min(nsm, ceil_div(mloc, 64))); }
+// Row splits of the W = V^T C step for ntiles column tiles.
+static int trail_splits(int mloc, int ntiles, int nsm) {
+  return std::max(1, std::min(std::min(64, ceil_div(2 * nsm, ntiles)), ceil_div(mloc, 128)));
+}
+
+size_t DmqrWorkspaceSizes::total(size_t align) const {
+  const size_t parts[] = {nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st,
+                          pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2};
+  size_t t = 0;
+  for (size_t b : parts) t += (b + align - 1) / align * align;
+  return t;
+}
+
+DmqrWorkspaceSizes dmqr_workspace_sizes(int m, int n, int nb, int nsm) {
+  DmqrWorkspaceSizes w;
+  const int minmn = std::min(m, n);
+  const int kcap = std::min(nb, minmn);
+  const int KM = kcap <= 64 ? 64 : 128;
+  const int KT = KM;
+  const int ntile1 = ceil_div(n, kTopkTile);
+  w.nrm = sizeof(double) * 2 * (size_t)n;
+  w.list = sizeof(int) * (size_t)n;
+  w.cand_a = sizeof(Cand) * (size_t)std::max(1, ntile1) * kcap + 64;
+  w.cand_b = sizeof(Cand) * (size_t)std::max(1, ceil_div(ntile1 * kcap, kTopkTile)) * kcap + 64;
+  w.cand = sizeof(Cand) * (size_t)KM;
+  w.gram_part = sizeof(double) * (size_t)gram_chunks_max(m, nsm) * KM * KM;
+  w.gram = sizeof(double) * (size_t)KM * KM;
+  w.perm = sizeof(int2) * (size_t)(2 * (2 * kcap + 2));
+  w.st = sizeof(BlockState);
+  const int gmax = panel_ctas(m, nsm);
+  w.pan_part = sizeof(double) * 2 * (size_t)gmax * (QRDM_NB_MAX + 1);
+  w.pan_row = sizeof(double) * 2 * (QRDM_NB_MAX + 2);
+  w.pan_bar = sizeof(unsigned) * 4;
+  w.vtv_part = sizeof(double) * (size_t)gmax * QRDM_NB_MAX * QRDM_NB_MAX;
+  w.vtv = sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX;
+  w.T = sizeof(double) * (size_t)KM * KM;
+  // the W = V^T C partials: max over the column-tile counts of a run
+  size_t wp = 0;
+  for (int nt = 1; nt <= std::max(1, ceil_div(n, 64)); ++nt)
+    wp = std::max(wp, (size_t)trail_splits(m, nt, nsm) * nt);
+  w.wpart = sizeof(double) * wp * KT * 64;
+  w.w2 = sizeof(double) * (size_t)KT * std::max(1, ceil_div(n, 64)) * 64;
+  return w;
+}
+
 // Panel geometry: G CTAs of R rows; returns false if the slab won't fit.
 static bool panel_geometry(const Ctx& c, int mloc, int kmax, int* G, int* R, size_t* smem) {
-  int g = std::max(1, std::min(c.nsm, ceil_div(mloc, 64)));
+  int g = panel_ctas(mloc, c.nsm);
   int r = ceil_div(mloc, g);
   size_t bytes = (size_t)r * kmax * sizeof(double);
   if (bytes + 8192 > c.smem_optin) return false;
@@ -170,9 +183,10 @@ static int apply_block_reflector(Ctx& c, cudaStream_t s, const double* V, long l
   if (ncols <= 0 || mloc <= 0) return 0;
   const int nsm = c.nsm;
   int ntiles = ceil_div(ncols, 64);
-  int nsplit = std::max(1, std::min(std::min(64, ceil_div(2 * nsm, ntiles)), ceil_div(mloc, 128)));
-  CK(c.wpart.ensure(sizeof(double) * (size_t)nsplit * 128 * ntiles * 64));
-  CK(c.w2.ensure(sizeof(double) * (size_t)128 * ntiles * 64));
+  int nsplit = trail_splits(mloc, ntiles, nsm);
+  const int KTb = kmax <= 64 ? 64 : 128;
+  CK(c.wpart.ensure(sizeof(double) * (size_t)nsplit * KTb * ntiles * 64));
+  CK(c.w2.ensure(sizeof(double) * (size_t)KTb * ntiles * 64));
   TrailArgs ta;
   ta.V = V;
   ta.ldv = ldv;
@@ -205,7 +219,7 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
                          const double* tau, int kmax, const BlockState* d_st) {
   int nchunk = std::max(1, std::min(c.nsm, ceil_div(mloc, 256)));
   int rpc = ceil_div(mloc, nchunk);
-  CK(c.vtv_part.ensure(sizeof(double) * (size_t)std::max(nchunk, c.nsm) * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.vtv_part.ensure(sizeof(double) * (size_t)nchunk * QRDM_NB_MAX * QRDM_NB_MAX));
   CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
   CK(c.T.ensure(sizeof(double) * (size_t)kmax * kmax));
   k_vtv_stored<<<nchunk, 256, 0, s>>>(V, ldv, mloc, rpc, d_st, c.vtv_part.as<double>());
@@ -219,11 +233,11 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
 }
 
 static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
-                         std::vector<int>& hj, int* err);
+                         int* hj, int* err);
 
 static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   cudaStream_t s = c.stream();
-  const bool timing = stats && stats->timing;
+  const bool timing = stats && stats->timing && c.ph[0] != nullptr;
   double ph_ms[5] = {0, 0, 0, 0, 0};
   double trail_flops = 0.0;
 #define PH(i)                                   \
@@ -238,33 +252,32 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   const int nsm = c.nsm;
 
   // ---- workspace
-  int ntile1 = ceil_div(n, kTopkTile);
-  CK(c.nrm.ensure(sizeof(double) * 2 * (size_t)n));
-  CK(c.list.ensure(sizeof(int) * (size_t)n));
-  CK(c.cand_a.ensure(sizeof(Cand) * (size_t)std::max(1, ntile1) * kcap + 64));
-  CK(c.cand_b.ensure(sizeof(Cand) * (size_t)std::max(1, ceil_div(ntile1 * kcap, kTopkTile)) * kcap + 64));
-  CK(c.cand.ensure(sizeof(Cand) * (size_t)KM));
-  const int max_chunks = 2 * nsm;
-  CK(c.gram_part.ensure(sizeof(double) * (size_t)max_chunks * KM * KM));
-  CK(c.gram.ensure(sizeof(double) * (size_t)KM * KM));
-  const int maxsw = 2 * kcap + 2;
-  CK(c.perm.ensure(sizeof(int2) * (size_t)(2 * maxsw)));
-  CK(c.st.ensure(sizeof(BlockState)));
-  CK(c.pan_part.ensure(sizeof(double) * 2 * (size_t)nsm * (QRDM_NB_MAX + 1)));
-  CK(c.pan_row.ensure(sizeof(double) * 2 * (QRDM_NB_MAX + 2)));
-  CK(c.pan_bar.ensure(sizeof(unsigned) * 4));
-  CK(c.vtv_part.ensure(sizeof(double) * (size_t)nsm * QRDM_NB_MAX * QRDM_NB_MAX));
-  CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
-  CK(c.T.ensure(sizeof(double) * (size_t)KM * KM));
-
-  CK(c.wpart.ensure(sizeof(double) * (size_t)(2 * nsm + ceil_div(n, 64)) * 128 * 64));
-  CK(c.w2.ensure(sizeof(double) * (size_t)128 * ceil_div(n, 64) * 64));
+  (void)KM;
+  const DmqrWorkspaceSizes ws = dmqr_workspace_sizes(m, n, nb, nsm);
+  CK(c.nrm.ensure(ws.nrm));
+  CK(c.list.ensure(ws.list));
+  CK(c.cand_a.ensure(ws.cand_a));
+  CK(c.cand_b.ensure(ws.cand_b));
+  CK(c.cand.ensure(ws.cand));
+  const int max_chunks = gram_chunks_max(m, nsm);
+  CK(c.gram_part.ensure(ws.gram_part));
+  CK(c.gram.ensure(ws.gram));
+  CK(c.perm.ensure(ws.perm));
+  CK(c.st.ensure(ws.st));
+  CK(c.pan_part.ensure(ws.pan_part));
+  CK(c.pan_row.ensure(ws.pan_row));
+  CK(c.pan_bar.ensure(ws.pan_bar));
+  CK(c.vtv_part.ensure(ws.vtv_part));
+  CK(c.vtv.ensure(ws.vtv));
+  CK(c.T.ensure(ws.T));
+  CK(c.wpart.ensure(ws.wpart));
+  CK(c.w2.ensure(ws.w2));
 
   BlockState* d_st = c.st.as<BlockState>();
   double* nrm = c.nrm.as<double>();
   double* nrm_exact = nrm + n;
 
-  CK(cudaEventRecord(c.ev0, s));
+  if (c.ev0) CK(cudaEventRecord(c.ev0, s));
   // ---- norm init (src/dgeqrdm_work.c:672-684) + NaN detection
   const int nfxd = P.nfxd;
   if (nfxd >= minmn) return 0;
@@ -408,11 +421,15 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     }
     if (P.kstop > 0 && j >= P.kstop) break;
   }
-  CK(cudaEventRecord(c.ev1, s));
-  CK(cudaEventSynchronize(c.ev1));
+  if (c.ev1) {
+    CK(cudaEventRecord(c.ev1, s));
+    CK(cudaEventSynchronize(c.ev1));
+  } else {
+    CK(cudaStreamSynchronize(s));
+  }
   if (stats) {
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, c.ev0, c.ev1);
+    if (c.ev0 && c.ev1) cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     stats->nblocks = it;
     stats->recomputes = recomputes;
     stats->rechecks = 0;
@@ -442,9 +459,9 @@ static int validate(int layout, int m, int n, int lda, const double* thres, int 
   return 0;
 }
 
-static int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, int* d_jpvt,
-                              double* d_tau, int* ncols, const double* thres, int nb,
-                              const qrdm_options* opt, qrdm_stats* stats) {
+int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, int* d_jpvt,
+                       double* d_tau, int* ncols, const double* thres, int nb,
+                       const qrdm_options* opt, qrdm_stats* stats, int* hj_buf) {
   int v = validate(layout, m, n, lda, thres, nb);
   if (v) return v;
   if (nb > QRDM_NB_MAX) return QRDM_ERR_UNSUPPORTED;
@@ -472,14 +489,20 @@ static int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int
   P.nancheck = o.nancheck;
   P.precision = o.precision;
   cudaStream_t s = c.stream();
-  std::vector<int> hj(n);
-  CK(cudaMemcpyAsync(hj.data(), d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  std::vector<int> hv;
+  int* hj = hj_buf;
+  if (!hj) {
+    hv.resize(n);
+    hj = hv.data();
+  }
+  CK(cudaMemcpyAsync(hj, d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   g_launches = 0;
   int err = 0;
   P.nfxd = fixed_columns(c, m, n, d_a, lda, d_tau, hj, &err);
   if (err) return err;
-  CK(cudaMemcpyAsync(d_jpvt, hj.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_jpvt, hj, sizeof(int) * n, cudaMemcpyHostToDevice, s));
+  CK(cudaStreamSynchronize(s));
   int r = dmqr_run(c, P, stats);
   if (stats) stats->launches = g_launches;
   return r;
@@ -493,12 +516,14 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
   cudaStream_t s = c.stream();
   const int k = std::min(m, n);
   const int nbq = 64;
-  CK(c.nrm.ensure(sizeof(double) * 2 * nbq));
+  const int gmax = panel_ctas(m, c.nsm);
+  const int nbn = std::min(nbq, k);  // column norms of one panel
+  CK(c.nrm.ensure(sizeof(double) * 2 * nbn));
   CK(c.st.ensure(sizeof(BlockState)));
-  CK(c.pan_part.ensure(sizeof(double) * 2 * (size_t)c.nsm * (QRDM_NB_MAX + 1)));
+  CK(c.pan_part.ensure(sizeof(double) * 2 * (size_t)gmax * (QRDM_NB_MAX + 1)));
   CK(c.pan_row.ensure(sizeof(double) * 2 * (QRDM_NB_MAX + 2)));
   CK(c.pan_bar.ensure(sizeof(unsigned) * 4));
-  CK(c.vtv_part.ensure(sizeof(double) * (size_t)c.nsm * QRDM_NB_MAX * QRDM_NB_MAX));
+  CK(c.vtv_part.ensure(sizeof(double) * (size_t)gmax * QRDM_NB_MAX * QRDM_NB_MAX));
   CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
   CK(c.T.ensure(sizeof(double) * nbq * nbq));
   BlockState* d_st = c.st.as<BlockState>();
@@ -506,7 +531,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
   for (int j = 0; j < k; j += nbq) {
     const int kb = std::min(nbq, k - j), mloc = m - j;
     k_block_init<<<1, 32, 0, s>>>(d_st, kb, 0);
-    k_colnorm_init<<<std::max(1, ceil_div(kb, 8)), 256, 0, s>>>(d_a, lda, j, mloc, j, kb, nrm, nrm + nbq, d_st);
+    k_colnorm_init<<<std::max(1, ceil_div(kb, 8)), 256, 0, s>>>(d_a, lda, j, mloc, j, kb, nrm, nrm + nbn, d_st);
     RET(check_launch());
     int G = 1, R = 1;
     size_t psmem = 0;
@@ -570,7 +595,7 @@ static int dormqr_locked(Ctx& c, int m, int n, int k, const double* d_a, long lo
 // pivoting, Q^T applied to the remaining columns.  Returns nfxd (>= 0) or
 // a negative/positive error code via *err.
 static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
-                         std::vector<int>& hj, int* err) {
+                         int* hj, int* err) {
   cudaStream_t s = c.stream();
   int nfxd = 0;
   *err = 0;
@@ -667,7 +692,7 @@ static int dgeqp3_locked(Ctx& c, int m, int n, double* d_a, long long lda, int* 
   CK(cudaStreamSynchronize(s));
   g_launches = 0;
   int err = 0;
-  const int nfxd = fixed_columns(c, m, n, d_a, lda, d_tau, hj, &err);
+  const int nfxd = fixed_columns(c, m, n, d_a, lda, d_tau, hj.data(), &err);
   if (err) return err;
   CK(cudaMemcpyAsync(d_jpvt, hj.data(), sizeof(int) * n, cudaMemcpyHostToDevice, s));
   if (nfxd >= minmn) return read_state(c, s);
@@ -724,7 +749,8 @@ int dgeqrdm_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jp
   Ctx* c = nullptr;
   int r = ctx_get(&c);
   if (r) return r;
-  return dgeqrdm_dev_locked(*c, matrix_layout, m, n, d_a, lda, d_jpvt, d_tau, ncols, thres, nb, opt, stats);
+  return dgeqrdm_dev_locked(*c, matrix_layout, m, n, d_a, lda, d_jpvt, d_tau, ncols, thres, nb, opt, stats,
+                            nullptr);
 }
 
 int dgeqrdm_ex(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, double* tau,
@@ -746,7 +772,7 @@ int dgeqrdm_ex(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, d
   CK(cudaMemcpyAsync(c->jpvt.p, jpvt, sizeof(int) * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->tau.p, tau, sizeof(double) * minmn, cudaMemcpyHostToDevice, s));
   r = dgeqrdm_dev_locked(*c, matrix_layout, m, n, d_a, m, c->jpvt.as<int>(), c->tau.as<double>(), ncols,
-                         thres, nb, opt, stats);
+                         thres, nb, opt, stats, nullptr);
   if (r > 0 || r == -1) return r;  // device failure or invalid argument: outputs untouched
   CK(cudaMemcpy2DAsync(a, sizeof(double) * (size_t)lda, d_a, sizeof(double) * m, sizeof(double) * m, n,
                        cudaMemcpyDeviceToHost, s));

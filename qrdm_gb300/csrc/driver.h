@@ -1,0 +1,82 @@
+// driver.h -- workspace and entry points of the host driver (internal to
+// libqrdm_gb300; not part of the C ABI).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstddef>
+#include <mutex>
+
+#include "../../include/qrdm_gb300.h"
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace qrdm {
+
+// ------------------------------------------------------------ workspace
+struct Buf {
+  void* p = nullptr;
+  size_t cap = 0;
+  bool view = false;  // fixed window of caller-provided memory: never (re)allocated
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (view) return cudaErrorMemoryAllocation;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t b = std::max<size_t>(bytes, 256);
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess) cap = b;
+    return e;
+  }
+  void release() {
+    if (p && !view) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <class T>
+  T* as() const {
+    return reinterpret_cast<T*>(p);
+  }
+};
+
+struct Ctx {
+  int dev = -1;
+  int nsm = 0;
+  size_t smem_optin = 0;
+  cudaStream_t own = nullptr;
+  cudaStream_t user = nullptr;
+  bool user_set = false;
+  Buf a, jpvt, tau;                        // device copies for host entry points
+  Buf nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st;
+  Buf pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
+  Buf qF, qg, qpart, qst;
+  BlockState* h_st = nullptr;              // pinned host copy of the block record
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ph[8] = {};
+  cudaStream_t stream() const { return user_set ? user : own; }
+};
+
+
+// DM-QR on device-resident data with the workspace of c.  hj: host scratch
+// of n ints (jpvt staging).  Caller holds the library lock.
+int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, int* d_jpvt,
+                       double* d_tau, int* ncols, const double* thres, int nb,
+                       const qrdm_options* opt, qrdm_stats* stats, int* hj);
+
+// Bytes of each workspace buffer DM-QR needs for an m x n problem with block
+// nb on a device with nsm SMs (used to carve a fixed scratch area).
+struct DmqrWorkspaceSizes {
+  size_t nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st;
+  size_t pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
+  size_t total(size_t align) const;
+};
+DmqrWorkspaceSizes dmqr_workspace_sizes(int m, int n, int nb, int nsm);
+
+// Function attributes (dynamic shared memory limits) for the current device.
+int set_kernel_attributes(int smem_optin);
+
+// The library-wide lock serialising host-side driver state.
+std::mutex& library_lock();
+
+}  // namespace qrdm
