@@ -94,6 +94,21 @@ int dgeqrdm_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jp
                 int* ncols, const double* thres, int nb, const qrdm_options* opt,
                 qrdm_stats* stats);
 
+/* dgeqrdm_dev for callers that cannot allocate device memory (inside a
+ * stream capture or a real-time loop where cudaMalloc would synchronise or
+ * fail, or inside a host application that owns every allocation).  No
+ * counterpart in the reference.  Allocates nothing: all scratch lives in one
+ * fixed 10 MiB device array inside the library, so problems are limited to
+ * m <= 1024, n <= 1024, nb <= 64 (larger sizes return QRDM_ERR_UNSUPPORTED
+ * with a message on stderr).  Options are the defaults (FP64, NaN scan).
+ * a, jpvt, tau are device pointers, ncols and thres host pointers; `stream`
+ * is a cudaStream_t (NULL: the legacy default stream).  The first call on a
+ * device looks up the array's device address and sets kernel attributes;
+ * make that first call before any stream capture.  Every call shares the
+ * array: calls that overlap on the GPU race and corrupt each other. */
+int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt,
+                        double* d_tau, int* ncols, const double* thres, int nb, void* stream);
+
 /* ------------------------------------------------------------------ QP3 */
 /* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot
  * per column by largest partial norm, first index on ties; jpvt[j] != 0

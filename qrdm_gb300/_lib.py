@@ -41,6 +41,8 @@ SIGNATURES = {
     "dgeqrdm_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                               C.c_void_p, _pi, _pd, C.c_int, C.POINTER(Options),
                               C.POINTER(Stats)]),
+    "dgeqrdm_dev_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
+                                      C.c_void_p, C.c_void_p, _pi, _pd, C.c_int, C.c_void_p]),
     "dgeqp3": (C.c_int, [C.c_int, C.c_int, C.c_int, _pd, C.c_int, _pi, _pd]),
     "dgeqp3_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                              C.c_void_p]),
