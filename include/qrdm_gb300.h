@@ -40,7 +40,7 @@ typedef struct qrdm_options {
   int precision;      /* QRDM_PREC_FP64 (default) or QRDM_PREC_MIXED             */
   int kstop;          /* > 0: stop once >= kstop columns are triangularised      */
   int nancheck;       /* 1 (default): scan the input for NaN, return -13         */
-  int slices;         /* Ozaki slices per operand (0 = default 7)                */
+  int slices;         /* Ozaki slices per operand, 4..7 (0 = default 7)          */
   double gram_margin; /* mixed Gram: |cos| within this of delta is recomputed in
                          FP64 (0 = default)                                      */
   int reserved[8];

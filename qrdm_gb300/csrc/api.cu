@@ -61,13 +61,14 @@ static int ctx_get(Ctx** out) {
 int set_kernel_attributes(int big) {
   {
     CK(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
+    CK(cudaFuncSetAttribute(k_panel_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
     CK(cudaFuncSetAttribute(k_topk_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkTile * (int)sizeof(Cand)));
-    CK(cudaFuncSetAttribute(k_topk_final, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkFinal * (int)sizeof(Cand)));
     CK(cudaFuncSetAttribute(k_dm_pick, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_permute_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_larft, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 2048));
     CK(cudaFuncSetAttribute(k_trail_w_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_qp3_gemv, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536));
+    if (oz_set_attributes()) return QRDM_ERR_CUDA;
   }
   return 0;
 }
@@ -93,7 +94,9 @@ struct DmqrProblem {
   int* ncols;    // host
   double delta, tau_rel, eta;
   int stop_mode, kstop, nancheck, precision;
-  int nfxd = 0;  // fixed leading columns already factored
+  int slices = 7;  // Ozaki digits per operand (mixed precision)
+  double gram_margin = 0.0078125;  // mixed Gram: FP64 recheck band around delta
+  int nfxd = 0;    // fixed leading columns already factored
 };
 
 #define RET(x)                 \
@@ -147,7 +150,7 @@ DmqrWorkspaceSizes dmqr_workspace_sizes(int m, int n, int nb, int nsm) {
   w.gram = sizeof(double) * (size_t)KM * KM;
   w.perm = sizeof(int2) * (size_t)(2 * (2 * kcap + 2));
   w.st = sizeof(BlockState);
-  const int gmax = panel_ctas(m, nsm);
+  const int gmax = ceil_div(panel_ctas(m, nsm), kPanelClusterSize) * kPanelClusterSize;
   w.pan_part = sizeof(double) * 2 * (size_t)gmax * (QRDM_NB_MAX + 1);
   w.pan_row = sizeof(double) * 2 * (QRDM_NB_MAX + 2);
   w.pan_bar = sizeof(unsigned) * 4;
@@ -227,13 +230,53 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
   int npair = kmax * (kmax - 1) / 2;
   k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), nchunk, d_st, c.vtv.as<double>());
   RET(check_launch());
-  k_larft<<<1, 256, sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), tau, d_st, c.T.as<double>(), kmax);
+  k_larft<<<1, 32 * ceil_div(4 * kmax, 32), sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), tau, d_st, c.T.as<double>(), kmax);
   RET(check_launch());
   return 0;
 }
 
 static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
                          int* hj, int* err);
+
+// Launch the Householder panel on the window of pa: the clustered kernel
+// when the device can co-schedule enough 8-CTA clusters, else the plain
+// cooperative kernel.  *G_used receives the number of CTAs (the count of
+// V^T V partials).
+static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t s, int* G_used) {
+  const int g0 = panel_ctas(mloc, c.nsm);
+  int ncl = ceil_div(g0, kPanelClusterSize);
+  for (int attempt = 0; attempt < 3 && ncl > 0; ++attempt) {
+    const int G = ncl * kPanelClusterSize;
+    const int R = ceil_div(mloc, G);
+    const size_t smem = (size_t)R * kmax * sizeof(double);
+    if (smem + 8192 > c.smem_optin) break;
+    const int cap = panel_cluster_capacity(smem);
+    if (cap <= 0) break;
+    if (ncl > cap) {
+      ncl = cap;
+      continue;
+    }
+    pa.rows_per_cta = R;
+    CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
+    if (launch_panel_cluster(pa, G, smem, s) == cudaSuccess) {
+      ++g_launches;
+      *G_used = G;
+      return 0;
+    }
+    cudaGetLastError();  // clear, fall back below
+    break;
+  }
+  int G = 1, R = 1;
+  size_t psmem = 0;
+  if (!panel_geometry(c, mloc, kmax, &G, &R, &psmem)) return QRDM_ERR_UNSUPPORTED;
+  pa.rows_per_cta = R;
+  CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
+  void* args[] = {&pa};
+  CK(cudaLaunchCooperativeKernel((void*)k_panel, dim3(G), dim3(256), args, psmem, s));
+  ++g_launches;
+  *G_used = G;
+  return 0;
+}
 
 static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   cudaStream_t s = c.stream();
@@ -272,6 +315,17 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   CK(c.T.ensure(ws.T));
   CK(c.wpart.ensure(ws.wpart));
   CK(c.w2.ensure(ws.w2));
+  const int slices = P.slices;
+  const bool mixed = P.precision == QRDM_PREC_MIXED;
+  if (mixed) {
+    size_t b1, b2, b3, b4, b5;
+    oz_workspace(m, n, slices, nsm, &b1, &b2, &b3, &b4, &b5);
+    CK(c.oz_va2.ensure(b1));
+    CK(c.oz_vb1.ensure(b2));
+    CK(c.oz_wb2.ensure(b3));
+    CK(c.oz_wexp.ensure(b4));
+    CK(c.oz_wp.ensure(b5));
+  }
 
   BlockState* d_st = c.st.as<BlockState>();
   double* nrm = c.nrm.as<double>();
@@ -294,14 +348,17 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   double maxnrm = bits_to_double(c.h_st->maxnrm_bits);
   double eta = P.eta * maxnrm;
 
-  int j = nfxd, it = 0, recomputes = 0;
+  int j = nfxd, it = 0, recomputes = 0, rechecks = 0;
   while (j < minmn) {
     const int mloc = m - j, nloc = n - j;
     const int kmax = std::min(std::min(nb, mloc), nloc);
     CK(cudaMemsetAsync(d_st, 0, sizeof(BlockState), s));
     PH(0);
     // ---- DM candidates (DM_perm :345-351)
-    {
+    if (nloc <= kTopkFinal) {
+      launch_topk_final(nloc, s, nullptr, nrm + j, kmax, P.tau_rel, c.cand.as<Cand>(), d_st);
+      RET(check_launch());
+    } else {
       const Cand* src = nullptr;
       int count = nloc;
       Cand* bufs[2] = {c.cand_a.as<Cand>(), c.cand_b.as<Cand>()};
@@ -319,25 +376,40 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
         src = bufs[which];
         count = tiles * kmax;
       }
-      k_topk_final<<<1, 1024, kTopkFinal * sizeof(Cand), s>>>(src, count, kmax, P.tau_rel, c.cand.as<Cand>(), d_st);
+      launch_topk_final(count, s, src, nullptr, kmax, P.tau_rel, c.cand.as<Cand>(), d_st);
       RET(check_launch());
     }
-    // ---- cosine matrix (DM_perm :365-379)
+    // ---- cosine matrix (DM_perm :365-379): FP64, or BF16 tensor cores
+    // with an FP64 recheck near delta in the mixed mode
     const int km = kmax <= 64 ? 64 : 128;
     {
-      int rows_per_chunk = std::max(32, ceil_div(mloc, max_chunks));
-      int nchunk = ceil_div(mloc, rows_per_chunk);
-      launch_gram_partial(km, nchunk, s, P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
-                          c.gram_part.as<double>());
-      RET(check_launch());
-      k_gram_reduce<<<ceil_div(km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
-      RET(check_launch());
+      if (mixed && km == 64) {
+        int rows_per_chunk = std::max(64, ceil_div(ceil_div(mloc, max_chunks), 64) * 64);
+        int nchunk = ceil_div(mloc, rows_per_chunk);
+        k_gram_bf16<<<nchunk, 128, 0, s>>>(P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
+                                           c.gram_part.as<double>());
+        RET(check_launch());
+        k_gram_reduce<<<ceil_div(km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
+        RET(check_launch());
+        const int npair = kmax * (kmax - 1) / 2;
+        k_gram_recheck<<<std::max(1, ceil_div(npair * 32, 256)), 256, 0, s>>>(
+            P.A, lda, j, mloc, c.cand.as<Cand>(), P.delta, P.gram_margin, km, d_st, c.gram.as<double>());
+        RET(check_launch());
+      } else {
+        int rows_per_chunk = std::max(32, ceil_div(mloc, max_chunks));
+        int nchunk = ceil_div(mloc, rows_per_chunk);
+        launch_gram_partial(km, nchunk, s, P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
+                            c.gram_part.as<double>());
+        RET(check_launch());
+        k_gram_reduce<<<ceil_div(km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
+        RET(check_launch());
+      }
     }
     // ---- greedy pick + permute_marked (DM_perm :382-415)
     {
       int msw = 2 * kmax + 2;
       size_t smem = sizeof(double) * 2 * msw + sizeof(int) * (2 * msw + 2 * kmax + 2 * msw) +
-                    sizeof(unsigned) * (size_t)ceil_div(nloc, 32) + 64;
+                    sizeof(unsigned) * ((size_t)ceil_div(nloc, 32) + 4) + sizeof(double) * (size_t)kmax * kmax + 64;
       if (smem + 1024 > c.smem_optin) return QRDM_ERR_UNSUPPORTED;
       k_dm_pick<<<1, 256, smem, s>>>(c.cand.as<Cand>(), c.gram.as<double>(), km, nloc, kmax, P.delta,
                                      P.jpvt + j, nrm + j, c.perm.as<int2>(), d_st);
@@ -349,11 +421,8 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     }
     PH(1);
     // ---- panel dgeqr2_mia (src/dgeqr2.c) with early exit
-    int G = 1, R = 1;
-    size_t psmem = 0;
-    if (!panel_geometry(c, mloc, kmax, &G, &R, &psmem)) return QRDM_ERR_UNSUPPORTED;
+    int G = 1;
     {
-      CK(cudaMemsetAsync(c.pan_bar.p, 0, sizeof(unsigned) * 4, s));
       PanelArgs pa;
       pa.A = P.A;
       pa.lda = lda;
@@ -367,11 +436,9 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       pa.rowbuf = c.pan_row.as<double>();
       pa.bar = c.pan_bar.as<unsigned>();
       pa.vtv_part = c.vtv_part.as<double>();
-      pa.rows_per_cta = R;
+      pa.rows_per_cta = 1;
       pa.allow_exit = 1;
-      void* args[] = {&pa};
-      CK(cudaLaunchCooperativeKernel((void*)k_panel, dim3(G), dim3(256), args, psmem, s));
-      ++g_launches;
+      RET(launch_panel(c, pa, mloc, kmax, s, &G));
     }
     PH(2);
     // ---- T factor (dlarft 'F','C', src/dgeqrdm_work.c:751-754)
@@ -379,14 +446,22 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       int npair = kmax * (kmax - 1) / 2;
       k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
       RET(check_launch());
-      k_larft<<<1, 256, sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), P.tau + j, d_st, c.T.as<double>(), kmax);
+      k_larft<<<1, 32 * ceil_div(4 * kmax, 32), sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), P.tau + j, d_st, c.T.as<double>(), kmax);
       RET(check_launch());
     }
     PH(3);
     // ---- trailing update (dlarfb 'L','T','F','C', src/dgeqrdm_work.c:762-767)
     {
       double* W0 = P.A + (size_t)j * lda + j;
-      RET(apply_block_reflector(c, s, W0, lda, W0, lda, mloc, nloc, 1, 1, kmax, d_st));
+      if (mixed && kmax <= 64) {
+        if (oz_trailing_update(s, W0, lda, mloc, nloc, nrm + j, c.T.as<double>(), kmax, slices, nsm, d_st,
+                               c.oz_va2.as<unsigned char>(), c.oz_vb1.as<unsigned char>(),
+                               c.oz_wb2.as<unsigned char>(), c.oz_wexp.as<int>(), c.oz_wp.as<double>(),
+                               &g_launches))
+          return QRDM_ERR_CUDA;
+      } else {
+        RET(apply_block_reflector(c, s, W0, lda, W0, lda, mloc, nloc, 1, 1, kmax, d_st));
+      }
     }
     PH(4);
     // ---- partial-norm downdate with recompute safeguard (norm_update)
@@ -414,6 +489,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     if (fjb_cmp <= 0 || fjb_cmp > hs.fjb) return QRDM_ERR_INTERNAL;
     P.ncols[it++] = fjb_cmp;
     recomputes += hs.recompute;
+    rechecks += hs.rechecks;
     maxnrm = bits_to_double(hs.maxnrm_bits);
     j += fjb_cmp;
     if (P.stop_mode >= 1 && P.stop_mode <= 3) {
@@ -432,7 +508,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     if (c.ev0 && c.ev1) cudaEventElapsedTime(&ms, c.ev0, c.ev1);
     stats->nblocks = it;
     stats->recomputes = recomputes;
-    stats->rechecks = 0;
+    stats->rechecks = rechecks;
     stats->columns = j;
     stats->ms_total = ms;
     stats->ms_select = ph_ms[0];
@@ -488,6 +564,10 @@ int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, i
   P.kstop = o.kstop;
   P.nancheck = o.nancheck;
   P.precision = o.precision;
+  if (o.precision != QRDM_PREC_FP64 && o.precision != QRDM_PREC_MIXED) return -1;
+  P.slices = o.slices == 0 ? 7 : o.slices;
+  P.gram_margin = o.gram_margin > 0.0 ? o.gram_margin : 0.0078125;
+  if (P.slices < 4 || P.slices > 7) return -1;
   cudaStream_t s = c.stream();
   std::vector<int> hv;
   int* hj = hj_buf;
@@ -516,7 +596,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
   cudaStream_t s = c.stream();
   const int k = std::min(m, n);
   const int nbq = 64;
-  const int gmax = panel_ctas(m, c.nsm);
+  const int gmax = ceil_div(panel_ctas(m, c.nsm), kPanelClusterSize) * kPanelClusterSize;
   const int nbn = std::min(nbq, k);  // column norms of one panel
   CK(c.nrm.ensure(sizeof(double) * 2 * nbn));
   CK(c.st.ensure(sizeof(BlockState)));
@@ -533,10 +613,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
     k_block_init<<<1, 32, 0, s>>>(d_st, kb, 0);
     k_colnorm_init<<<std::max(1, ceil_div(kb, 8)), 256, 0, s>>>(d_a, lda, j, mloc, j, kb, nrm, nrm + nbn, d_st);
     RET(check_launch());
-    int G = 1, R = 1;
-    size_t psmem = 0;
-    if (!panel_geometry(c, mloc, kb, &G, &R, &psmem)) return QRDM_ERR_UNSUPPORTED;
-    CK(cudaMemsetAsync(c.pan_bar.p, 0, sizeof(unsigned) * 4, s));
+    int G = 1;
     PanelArgs pa;
     pa.A = d_a;
     pa.lda = lda;
@@ -550,14 +627,12 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
     pa.rowbuf = c.pan_row.as<double>();
     pa.bar = c.pan_bar.as<unsigned>();
     pa.vtv_part = c.vtv_part.as<double>();
-    pa.rows_per_cta = R;
+    pa.rows_per_cta = 1;
     pa.allow_exit = 0;
-    void* args[] = {&pa};
-    CK(cudaLaunchCooperativeKernel((void*)k_panel, dim3(G), dim3(256), args, psmem, s));
-    ++g_launches;
+    RET(launch_panel(c, pa, mloc, kb, s, &G));
     int npair = kb * (kb - 1) / 2;
     k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
-    k_larft<<<1, 256, sizeof(double) * (size_t)kb * kb, s>>>(c.vtv.as<double>(), d_tau + j, d_st, c.T.as<double>(), kb);
+    k_larft<<<1, 32 * ceil_div(4 * kb, 32), sizeof(double) * (size_t)kb * kb, s>>>(c.vtv.as<double>(), d_tau + j, d_st, c.T.as<double>(), kb);
     RET(check_launch());
     double* W0 = d_a + (size_t)j * lda + j;
     RET(apply_block_reflector(c, s, W0, lda, W0 + (size_t)kb * lda, lda, mloc, n - j - kb, 0, 1, kb, d_st));
@@ -944,7 +1019,8 @@ int qrdm_release_workspace(void) {
   Ctx& c = g_ctx[dev];
   Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
                  &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
-                 &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst};
+                 &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst,
+                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp};
   for (Buf* b : bufs) b->release();
   return 0;
 }

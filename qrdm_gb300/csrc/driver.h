@@ -51,6 +51,7 @@ struct Ctx {
   Buf nrm, list, cand_a, cand_b, cand, gram_part, gram, perm, st;
   Buf pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
   Buf qF, qg, qpart, qst;
+  Buf oz_va2, oz_vb1, oz_wb2, oz_wexp, oz_wp;  // mixed-precision trailing update
   BlockState* h_st = nullptr;              // pinned host copy of the block record
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ph[8] = {};

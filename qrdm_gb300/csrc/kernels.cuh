@@ -60,13 +60,17 @@ __global__ void k_norm_recompute(const double* A, long long lda, int j, int m, c
 // select.cu
 __global__ void k_topk_tile(const double* nrm, const Cand* in_cand, int count, int kmax,
                             Cand* out);
-__global__ void k_topk_final(const Cand* in_cand, int count, int kmax, double tau_rel, Cand* cand,
-                             BlockState* st);
+void launch_topk_final(int count, cudaStream_t st_, const Cand* in_cand, const double* nrm, int kmax,
+                       double tau_rel, Cand* cand, BlockState* st);
 void launch_gram_partial(int km, int nchunk, cudaStream_t s, const double* A, long long lda, int j,
                          int mloc, int rows_per_chunk, const Cand* cand, const BlockState* st,
                          double* part);
 __global__ void k_gram_reduce(const double* part, int nchunk, int km, const BlockState* st,
                               double* gram);
+__global__ void k_gram_bf16(const double* A, long long lda, int j, int mloc, int rows_per_chunk,
+                            const Cand* cand, BlockState* st, double* part);
+__global__ void k_gram_recheck(const double* A, long long lda, int j, int mloc, const Cand* cand,
+                               double delta, double margin, int km, BlockState* st, double* gram);
 __global__ void k_dm_pick(const Cand* cand, const double* gram, int km, int ncols, int kmax,
                           double delta, int* jpvt, double* nrm, int2* perm, BlockState* st);
 __global__ void k_permute_columns(double* A, long long lda, int m, int j, const int2* perm,
@@ -77,6 +81,10 @@ __global__ void k_block_init(BlockState* st, int fjb, int fjb_cmp);
 __global__ void k_vtv_stored(const double* V, long long ldv, int mloc, int rows_per_chunk,
                              const BlockState* st, double* vtv_part);
 __global__ void k_panel(PanelArgs p);
+__global__ void k_panel_cluster(PanelArgs p);
+cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, size_t smem, cudaStream_t s);
+int panel_cluster_capacity(size_t smem);
+constexpr int kPanelClusterSize = 8;
 __global__ void k_vtv_reduce(const double* vtv_part, int G, const BlockState* st, double* vtv);
 __global__ void k_larft(const double* vtv, const double* tau, const BlockState* st, double* T,
                         int ldt);
@@ -85,6 +93,14 @@ __global__ void k_larft(const double* vtv, const double* tau, const BlockState* 
 void launch_trail_w_partial(int KT, dim3 grid, cudaStream_t s, const TrailArgs& a);
 __global__ void k_trail_w_reduce(TrailArgs p, int nsplit, int KT);
 __global__ void k_trail_update(TrailArgs p);
+
+// ozaki.cu
+int oz_set_attributes();
+int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
+                       const double* T, int ldt, int s, int nsm, BlockState* st, unsigned char* va2,
+                       unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp, int* launches);
+void oz_workspace(int m, int n, int s, int nsm, size_t* va2, size_t* vb1, size_t* wb2, size_t* wexp,
+                  size_t* wp);
 
 // qp3.cu
 struct Qp3State;

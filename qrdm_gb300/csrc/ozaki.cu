@@ -1,0 +1,583 @@
+// ozaki.cu -- FP64-accurate trailing update on the BF16 tensor cores.
+//
+// Replaces the FP64 dlarfb (src/dgeqrdm_work.c:762-767) in the mixed
+// precision mode:   W = V^T C,  W2 = T^T W,  C -= V W2.
+//
+// Split (Ozaki, Ogita, Oishi & Rump, "Error-free transformations of matrix
+// multiplication by using fast routines of matrix multiplication", 2012):
+// every FP64 operand x is written, relative to a power-of-two scale 2^e
+// shared along the dot-product direction, as s base-256 balanced digits
+//     x ~= 2^e * sum_{p=1..s} d_p 256^-p,   d_p integer, |d_p| <= 128,
+// each exactly representable in BF16.  A product of two matrices becomes
+// sum over digit pairs (p, q) of exact BF16 products accumulated in FP32 on
+// tcgen05; pairs with p + q > s + 1 are dropped (their weight is below
+// 256^-(s+1)).  Pairs of equal level L = p + q share one TMEM accumulator
+// (level-major columns), so one MMA with the B digits q = 1..Q stacked along
+// N feeds Q consecutive levels at once.  Products are bounded by 2^14, so a
+// level holding c pairs over K terms is an exact FP32 integer while
+// c K 2^14 <= 2^24; levels 2..5 (the ones whose rounding would matter) stay
+// exact for K <= 256, which is the drain interval of the long-K product.
+// Levels are recombined in integer arithmetic (int64 for levels 2..5, a
+// second word for 6..s+1) and only the final value touches the FP64 pipe:
+// GB300's FP64 rate (~2 FMA/clk/SM) is the scarce resource here.
+//
+// Scales: Householder vectors satisfy |v| <= 1 (|x_r| <= |alpha - beta|), so V
+// uses the fixed scale 2^1.  The columns of C use 2^(E+1) with E the binary
+// exponent of their partial norm (an upper bound of every entry).  The
+// columns of W2 use 2^(E+1) of their own max.
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+#include "kernels.cuh"
+#include "tc.cuh"
+
+namespace qrdm {
+
+constexpr int OZ_TPB = 256;
+constexpr int OZ_MAXS = 8;
+
+// round(x * 2^sh) as int64 (|result| < 2^62 by the caller's choice of sh)
+__device__ __forceinline__ long long fixed_point(double x, int sh) {
+  unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  int E = (int)((b >> 52) & 0x7FF);
+  long long M = (long long)(b & 0xFFFFFFFFFFFFFull);
+  int e2;
+  if (E == 0) {
+    e2 = -1074 + sh;
+  } else {
+    M |= (1ll << 52);
+    e2 = E - 1075 + sh;
+  }
+  long long F;
+  if (e2 >= 0) {
+    F = M << (e2 > 62 ? 62 : e2);
+  } else if (e2 < -60) {
+    F = 0;
+  } else {
+    F = (M + (1ll << (-e2 - 1))) >> (-e2);
+  }
+  return (b >> 63) ? -F : F;
+}
+
+// s balanced base-256 digits of F (d[0] most significant), |d| <= 128.
+__device__ __forceinline__ void balanced_digits(long long F, int s, int* d) {
+#pragma unroll
+  for (int p = OZ_MAXS - 1; p >= 1; --p) {
+    if (p < s) {
+      int r = (int)(F & 255);
+      if (r >= 128) r -= 256;
+      d[p] = r;
+      F = (F - r) >> 8;
+    }
+  }
+  d[0] = (int)F;
+}
+
+// |d| <= 256 integer -> FP32 exactly via the 1.5 * 2^23 shifter (one integer
+// add, one FP32 add), whose upper 16 bits are its exact BF16 encoding.
+__device__ __forceinline__ uint32_t digit_f32_bits(int d) {
+  return __float_as_uint(__int_as_float(0x4B400000 + d) - 12582912.0f);
+}
+__device__ __forceinline__ uint32_t pack2_bf16(int lo, int hi) {
+  return (digit_f32_bits(lo) >> 16) | (digit_f32_bits(hi) & 0xFFFF0000u);
+}
+__device__ __forceinline__ unsigned short bf16_bits(int d) {
+  return (unsigned short)(digit_f32_bits(d) >> 16);
+}
+// exact FP32 integer (|x| < 2^31) -> int32
+__device__ __forceinline__ int f32_to_int(float x) { return __float2int_rn(x); }
+// 2^e as a double (normal range), built from its bit pattern
+__device__ __forceinline__ double pow2d(int e) {
+  e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
+  return __longlong_as_double((long long)(e + 1023) << 52);
+}
+
+__device__ __forceinline__ int scale_exp_of(double bound) {
+  if (!(bound > 0.0) || !(bound < 1.7976931348623157e308)) return 0;
+  int e;
+  frexp(bound, &e);
+  return e + 1;  // |x| <= bound < 2^e  ->  |x| / 2^(e+1) < 1/2
+}
+
+// ------------------------------------------------------------- V digits
+// V (mloc x k, unit lower trapezoidal, window origin V) -> digit tiles:
+//   va2[t][p]: rows 128t..128t+127, K = the 64 reflector columns (GEMM2 A)
+//   vb1[b][p]: N = the 64 reflector columns, K = rows 64b..64b+63 (GEMM1 B)
+// fixed scale 2^1.  One thread per (row, pair of reflector columns).
+__global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict__ V, long long ldv,
+                                                        int mloc, int s, const BlockState* __restrict__ st,
+                                                        unsigned char* __restrict__ va2,
+                                                        unsigned char* __restrict__ vb1) {
+  const int k = st->fjb_cmp;
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  const int mpad = ceil_div(mloc, 256) * 256;
+  if (e >= (long long)mpad * 32) return;
+  const int r = (int)(e / 32), ap = (int)(e % 32);  // row, column pair
+  const int sh = 8 * s - 1;
+  int dg[2][OZ_MAXS];
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    const int a = 2 * ap + h;
+    double v = 0.0;
+    if (r < mloc && a < k) v = r > a ? V[(size_t)a * ldv + r] : (r == a ? 1.0 : 0.0);
+    balanced_digits(fixed_point(v, sh), s, dg[h]);
+  }
+  const int t = r >> 7, rr = r & 127;
+  for (int p = 0; p < s; ++p) {
+    // GEMM2 A tile: row rr, K = a (pair packed)
+    unsigned char* ta = va2 + ((size_t)t * s + p) * 16384;
+    *reinterpret_cast<uint32_t*>(ta + tc::sw128_offset(rr, 2 * ap)) = pack2_bf16(dg[0][p], dg[1][p]);
+  }
+  // GEMM1 B tile: row (N) = a, K = r % 64 -- the two reflector columns land in
+  // different rows; store 16-bit values
+  const int b = r >> 6, kr = r & 63;
+  for (int p = 0; p < s; ++p) {
+    unsigned char* tb = vb1 + ((size_t)b * s + p) * 8192;
+#pragma unroll
+    for (int h = 0; h < 2; ++h)
+      *reinterpret_cast<unsigned short*>(tb + tc::sw128_offset(2 * ap + h, kr)) = bf16_bits(dg[h][p]);
+  }
+}
+
+// ------------------------------------------------------- shared helpers
+// Issue the digit-pair MMAs of one 64-deep K block: A digits at a_tiles
+// (s tiles of 128 x 64, stride a_stride), B digits stacked at b_tiles
+// (s tiles of 64 rows, 8 KB each); level L = p + q (1-based digits) lands in
+// TMEM columns (L - 2) * 64.  first: overwrite instead of accumulate.
+__device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32_t a_stride, uint32_t b_tiles,
+                                         int s, bool first) {
+  for (int p = 1; p <= s; ++p) {
+    const int Q = s + 1 - p;  // q = 1..Q
+    for (int q0 = 1; q0 <= Q; q0 += 4) {
+      const int nq = min(4, Q - q0 + 1);
+      const uint32_t idesc = tc::idesc_bf16_f32(128, 64 * nq);
+      const uint32_t dcol = (uint32_t)((p + q0 - 2) * 64);
+      for (int kk = 0; kk < 4; ++kk) {
+        uint64_t ad = tc::desc_sw128(a_tiles + (uint32_t)(p - 1) * a_stride + kk * 32);
+        uint64_t bd = tc::desc_sw128(b_tiles + (uint32_t)(q0 - 1) * 8192u + kk * 32);
+        tc::mma_bf16(tmem + dcol, ad, bd, idesc, (first && p == 1 && kk == 0) ? 0u : 1u);
+      }
+    }
+  }
+}
+
+// Load the s levels of 8 accumulator columns (col0..col0+7) of this thread's
+// TMEM lane and combine them: hi = sum_{L<=5} D_L 2^(8(5-L)) (exact int64),
+// mid = sum_{L>=6} D_L 2^(8(s+1-L)) (int64 of exact or nearly exact values).
+__device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, int s, long long* hi,
+                                           long long* mid) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    hi[i] = 0;
+    mid[i] = 0;
+  }
+  for (int L = 2; L <= s + 1; ++L) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr_lane + (uint32_t)((L - 2) * 64 + col0))
+                 : "memory");
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      long long v = (long long)f32_to_int(__uint_as_float(r[i]));
+      if (L <= 5) hi[i] += v << (8 * (5 - L));
+      else mid[i] += v << (8 * (s + 1 - L));
+    }
+  }
+}
+
+// ------------------------------------------------------------- GEMM 1
+// Partial W^T tile: 128 columns of C x the k (<= 64) reflector columns,
+// over the 256-row chunks [chunk_begin, chunk_end) of the window.
+// Wp[split][c][a] (FP64).  C columns start at window column st->fjb.
+struct OzG1Args {
+  const double* W0;     // window origin A(j, j)
+  long long lda;
+  int mloc, ncols;      // window rows / columns
+  const double* nrm;    // partial norms, window-relative
+  const unsigned char* vb1;
+  int s;
+  int chunks_per_split;
+  double* Wp;           // [split][npad][64]
+  int npad;
+  BlockState* st;
+};
+
+__global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int s = g.s;
+  unsigned char* adig = base;                  // s x 16 KB
+  unsigned char* bdig = base + s * 16384;      // s x 8 KB
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  __shared__ int s_e[128];
+  const int fjb = g.st->fjb;
+  const int k = g.st->fjb_cmp;
+  const int c0 = fjb + blockIdx.x * 128;  // first window column of this tile
+  if (c0 >= g.ncols || k <= 0) return;
+  const int nchunk = ceil_div(g.mloc, 256);
+  const int ch_begin = blockIdx.y * g.chunks_per_split;
+  const int ch_end = min(nchunk, ch_begin + g.chunks_per_split);
+  const int tid = threadIdx.x;
+  if (tid < 128) {
+    const int c = c0 + tid;
+    s_e[tid] = c < g.ncols ? scale_exp_of(g.nrm[c]) : 0;
+  }
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (tid < 32) tc::tmem_alloc(&s_tmem, 512);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  const int w = tid >> 5, lane = tid & 31;
+  const int row = 32 * (w & 3) + lane;  // TMEM lane = tile row = C column (c0 + row)
+  const int half = tid >> 7;            // reflector columns [32 half, 32 half + 32)
+  const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
+  long long acc_hi[32];
+  float acc_mid[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    acc_hi[i] = 0;
+    acc_mid[i] = 0.f;
+  }
+  uint32_t phase = 0;
+  bool ok = true;
+  for (int ch = ch_begin; ch < ch_end && ok; ++ch) {
+    for (int kb = 0; kb < 4; ++kb) {
+      const int r0 = ch * 256 + kb * 64;
+      // C rows r0..r0+63 x columns c0..c0+127 -> A digit tiles (row = column of C)
+      // 16 row pairs per thread, loaded 4 at a time before any conversion so
+      // the global loads overlap (the conversion is latency-bound otherwise)
+#pragma unroll 1
+      for (int it = 0; it < 16; it += 4) {
+        double2 xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = tid + OZ_TPB * (it + u);
+          const int rp = e & 31, cc = e >> 5;
+          const int c = c0 + cc, r = r0 + 2 * rp;
+          xv[u] = make_double2(0.0, 0.0);
+          if (c < g.ncols) {
+            const double* col = g.W0 + (size_t)c * g.lda;
+            if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
+              xv[u] = __ldg(reinterpret_cast<const double2*>(col + r));
+            } else {
+              if (r < g.mloc) xv[u].x = __ldg(col + r);
+              if (r + 1 < g.mloc) xv[u].y = __ldg(col + r + 1);
+            }
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int e = tid + OZ_TPB * (it + u);
+          const int rp = e & 31, cc = e >> 5;
+          const int sh = 8 * s - s_e[cc];
+          int d0[OZ_MAXS], d1[OZ_MAXS];
+          balanced_digits(fixed_point(xv[u].x, sh), s, d0);
+          balanced_digits(fixed_point(xv[u].y, sh), s, d1);
+          const uint32_t off = tc::sw128_offset(cc, 2 * rp);
+#pragma unroll
+          for (int p = 0; p < OZ_MAXS; ++p)
+            if (p < s) *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+        }
+      }
+      // V digits of this 64-row block (GEMM1 B tiles, contiguous s x 8 KB)
+      {
+        const int b = r0 >> 6;
+        const uint4* src = reinterpret_cast<const uint4*>(g.vb1 + (size_t)b * s * 8192);
+        uint4* dst = reinterpret_cast<uint4*>(bdig);
+        for (int e = tid; e < s * 512; e += OZ_TPB) dst[e] = src[e];
+      }
+      tc::fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        oz_issue(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig), s, kb == 0);
+        tc::mma_commit(&bar);
+      }
+      if (!tc::mbar_wait(&bar, phase)) {
+        atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+        ok = false;
+      }
+      phase ^= 1u;
+      tc::fence_after_sync();
+    }
+    if (!ok) break;
+    // drain the chunk's levels into the integer accumulators
+#pragma unroll
+    for (int g8 = 0; g8 < 4; ++g8) {
+      long long hi[8], mid[8];
+      oz_levels8(taddr, 32 * half + 8 * g8, s, hi, mid);
+#pragma unroll
+      for (int i = 0; i < 8; ++i) {
+        acc_hi[8 * g8 + i] += hi[i];
+        acc_mid[8 * g8 + i] += (float)mid[i];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(s+1))
+  if (ok) {
+    const int c = c0 + row;
+    double* out = g.Wp + ((size_t)blockIdx.y * g.npad + (size_t)(c - fjb)) * 64;
+    if (c < g.ncols) {
+      const int e = s_e[row];
+#pragma unroll
+      for (int i = 0; i < 32; ++i) {
+        const int a = 32 * half + i;
+        double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (s + 1)));
+        out[a] = a < k ? v : 0.0;
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < 32) tc::tmem_dealloc(tmem, 512);
+}
+
+// ------------------------------------------- W2 = T^T W and its digits
+// One CTA per 16 C-columns (a quarter of a 64-row GEMM2 B tile): sum the
+// split partials (fixed order), apply T^T, then slice W2 per column (scale
+// 2^(E+1) of the column max) into the GEMM2 B tiles wb2[tile][q]
+// (N = C column, K = reflector column).
+constexpr int OZ_W2_COLS = 16;
+
+__global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp, int nsplit, int npad,
+                                                   const double* __restrict__ T, int ldt, int ncols,
+                                                   int s, const BlockState* __restrict__ st,
+                                                   unsigned char* __restrict__ wb2, int* __restrict__ wexp) {
+  __shared__ double sW[OZ_W2_COLS][65];  // [c][a]
+  __shared__ double sT[64][65];          // T(b, a) at [a][b]
+  __shared__ double smax[OZ_W2_COLS];
+  const int k = st->fjb_cmp;
+  const int ncols_c = ncols - st->fjb;  // columns of C
+  const int cbase = blockIdx.x * OZ_W2_COLS;
+  if (cbase >= ncols_c || k <= 0) return;
+  for (int e = threadIdx.x; e < OZ_W2_COLS * 64; e += blockDim.x) {
+    const int cc = e / 64, a = e % 64;
+    double acc = 0.0;
+    if (a < k && cbase + cc < ncols_c)
+      for (int q = 0; q < nsplit; ++q) acc += Wp[((size_t)q * npad + cbase + cc) * 64 + a];
+    sW[cc][a] = acc;
+  }
+  for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+    const int a = e / 64, b = e % 64;
+    sT[a][b] = (a < k && b < k) ? T[(size_t)a * ldt + b] : 0.0;
+  }
+  __syncthreads();
+  // W2(a, c) = sum_{b <= a} T(b, a) W(b, c)
+  double w2[4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int e = threadIdx.x + OZ_TPB * i;  // 0..1023
+    const int cc = e / 64, a = e % 64;
+    double acc = 0.0;
+    if (a < k)
+      for (int b = 0; b <= a; ++b) acc = fma(sT[a][b], sW[cc][b], acc);
+    w2[i] = acc;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int e = threadIdx.x + OZ_TPB * i;
+    sW[e / 64][e % 64] = w2[i];
+  }
+  __syncthreads();
+  if (threadIdx.x < OZ_W2_COLS) {
+    double mx = 0.0;
+    for (int a = 0; a < 64; ++a) mx = fmax(mx, fabs(sW[threadIdx.x][a]));
+    smax[threadIdx.x] = mx;
+    if (cbase + threadIdx.x < ncols_c) wexp[cbase + threadIdx.x] = scale_exp_of(mx);
+  }
+  __syncthreads();
+  // digits: thread -> (column cc, reflector pair ap); tile rows = columns
+  const int tile = cbase / 64, row0 = cbase % 64;
+  for (int e = threadIdx.x; e < OZ_W2_COLS * 32; e += blockDim.x) {
+    const int cc = e / 32, ap = e % 32;
+    const int sh = 8 * s - scale_exp_of(smax[cc]);
+    int d0[OZ_MAXS], d1[OZ_MAXS];
+    balanced_digits(fixed_point(sW[cc][2 * ap], sh), s, d0);
+    balanced_digits(fixed_point(sW[cc][2 * ap + 1], sh), s, d1);
+    const uint32_t off = tc::sw128_offset(row0 + cc, 2 * ap);
+#pragma unroll
+    for (int q = 0; q < OZ_MAXS; ++q)
+      if (q < s)
+        *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * s + q) * 8192 + off) = pack2_bf16(d0[q], d1[q]);
+  }
+}
+
+// ------------------------------------------------------------- GEMM 2
+// C(r, c) -= V(r, :) W2(:, c) for a 128-row x 64-column tile of C
+// (C columns start at window column st->fjb).
+struct OzG2Args {
+  double* W0;
+  long long lda;
+  int mloc, ncols;
+  const unsigned char* va2;
+  const unsigned char* wb2;
+  const int* wexp;
+  int s;
+  BlockState* st;
+};
+
+
+__global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
+  extern __shared__ unsigned char smem_raw[];
+  unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const int s = g.s;
+  unsigned char* adig = base;              // s x 16 KB
+  unsigned char* bdig = base + s * 16384;  // s x 8 KB
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  const int fjb = g.st->fjb;
+  const int k = g.st->fjb_cmp;
+  const int ct = blockIdx.x, rt = blockIdx.y;
+  const int cw0 = ct * 64;  // first C column relative to fjb
+  if (fjb + cw0 >= g.ncols || rt * 128 >= g.mloc || k <= 0) return;
+  const int tid = threadIdx.x;
+  {
+    const uint4* sa = reinterpret_cast<const uint4*>(g.va2 + (size_t)rt * s * 16384);
+    uint4* da = reinterpret_cast<uint4*>(adig);
+    for (int e = tid; e < s * 1024; e += OZ_TPB) da[e] = sa[e];
+    const uint4* sb = reinterpret_cast<const uint4*>(g.wb2 + (size_t)ct * s * 8192);
+    uint4* db = reinterpret_cast<uint4*>(bdig);
+    for (int e = tid; e < s * 512; e += OZ_TPB) db[e] = sb[e];
+  }
+  tc::fence_async_smem();
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (tid < 32) tc::tmem_alloc(&s_tmem, 512);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  if (tid == 0) {
+    oz_issue(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig), s, true);
+    tc::mma_commit(&bar);
+  }
+  const int w = tid >> 5, lane = tid & 31;
+  const int rr = 32 * (w & 3) + lane;
+  const int half = tid >> 7;
+  const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
+  const int r = rt * 128 + rr;
+  // fetch this thread's 32 entries of C while the tensor core works
+  double cv[32];
+#pragma unroll
+  for (int i = 0; i < 32; ++i) {
+    const int c = fjb + cw0 + 32 * half + i;
+    cv[i] = (r < g.mloc && c < g.ncols) ? g.W0[(size_t)c * g.lda + r] : 0.0;
+  }
+  const bool ok = tc::mbar_wait(&bar, 0);
+  if (!ok) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+  tc::fence_after_sync();
+  if (ok) {
+#pragma unroll
+    for (int g8 = 0; g8 < 4; ++g8) {
+      long long hi[8], mid[8];
+      oz_levels8(taddr, 32 * half + 8 * g8, s, hi, mid);
+      if (r < g.mloc) {
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          const int cw = cw0 + 32 * half + 8 * g8 + i;
+          const int c = fjb + cw;
+          if (c < g.ncols) {
+            const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
+            // U = 2^e (hi 256^-5 + mid 256^-(s+1)).  hi < 2^45 and
+            // mid < 2^40, so hi 2^17 + mid 2^(57-8s) fits in 62 bits and keeps
+            // ~2^-62 of U: one conversion, one FP64 subtraction.
+            const int msh = 8 * (s + 1) - 40 - 17;  // weight of mid relative to hi 2^17
+            const long long comb = (hi[i] << 17) + (msh >= 0 ? (mid[i] >> msh) : (mid[i] << -msh));
+            const double u = (double)comb * pow2d(e - 40 - 17);
+            g.W0[(size_t)c * g.lda + r] = cv[8 * g8 + i] - u;
+          }
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < 32) tc::tmem_dealloc(tmem, 512);
+}
+
+// ------------------------------------------------------------ launchers
+size_t oz_gemm_smem(int s) { return (size_t)s * (16384 + 8192) + 1024; }
+
+int oz_set_attributes() {
+  const int bytes = (int)oz_gemm_smem(OZ_MAXS);
+  if (cudaFuncSetAttribute(k_oz_gemm1, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+    return 1;
+  if (cudaFuncSetAttribute(k_oz_gemm2, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+    return 1;
+  return 0;
+}
+
+// Whole mixed-precision trailing update of one DM block.  Buffers: va2/vb1
+// (V digits), wb2 (W2 digits), wexp (n ints), Wp (nsplit x npad x 64 FP64).
+int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
+                       const double* T, int ldt, int s, int nsm, BlockState* st, unsigned char* va2,
+                       unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp, int* launches) {
+  if (ncols <= 1 || mloc <= 0) return 0;
+  const int mpad = ceil_div(mloc, 256) * 256;
+  k_oz_slice_v<<<ceil_div(mpad * 32, OZ_TPB), OZ_TPB, 0, st_>>>(W0, lda, mloc, s, st, va2, vb1);
+  const int ctiles = ceil_div(ncols - 1, 128);  // >= 1 column is selected
+  const int nchunk = ceil_div(mloc, 256);
+  int nsplit = std::max(1, std::min(nchunk, ceil_div(2 * nsm, ctiles)));
+  const int cps = ceil_div(nchunk, nsplit);
+  nsplit = ceil_div(nchunk, cps);
+  const int npad = ctiles * 128;
+  OzG1Args a1;
+  a1.W0 = W0;
+  a1.lda = lda;
+  a1.mloc = mloc;
+  a1.ncols = ncols;
+  a1.nrm = nrm;
+  a1.vb1 = vb1;
+  a1.s = s;
+  a1.chunks_per_split = cps;
+  a1.Wp = Wp;
+  a1.npad = npad;
+  a1.st = st;
+  k_oz_gemm1<<<dim3(ctiles, nsplit), OZ_TPB, oz_gemm_smem(s), st_>>>(a1);
+  const int wtiles = ceil_div(ncols - 1, 64);
+  k_oz_w2<<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nsplit, npad, T, ldt, ncols, s, st, wb2,
+                                                                wexp);
+  OzG2Args a2;
+  a2.W0 = W0;
+  a2.lda = lda;
+  a2.mloc = mloc;
+  a2.ncols = ncols;
+  a2.va2 = va2;
+  a2.wb2 = wb2;
+  a2.wexp = wexp;
+  a2.s = s;
+  a2.st = st;
+  k_oz_gemm2<<<dim3(wtiles, ceil_div(mloc, 128)), OZ_TPB, oz_gemm_smem(s), st_>>>(a2);
+  if (launches) *launches += 4;
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+// Workspace bytes of the mixed trailing update for an m x n problem.
+void oz_workspace(int m, int n, int s, int nsm, size_t* va2, size_t* vb1, size_t* wb2, size_t* wexp,
+                  size_t* wp) {
+  *va2 = (size_t)ceil_div(m, 256) * 2 * s * 16384;
+  *vb1 = (size_t)ceil_div(m, 256) * 4 * s * 8192;
+  *wb2 = (size_t)ceil_div(n, 64) * s * 8192;
+  *wexp = sizeof(int) * (size_t)n;
+  const int ctiles = ceil_div(n, 128);
+  const int nchunk = ceil_div(m, 256);
+  int maxsplit = 1;
+  for (int ct = 1; ct <= ctiles; ++ct)
+    maxsplit = std::max(maxsplit, std::min(nchunk, ceil_div(2 * nsm, ct)) * ct);
+  *wp = sizeof(double) * (size_t)maxsplit * 128 * 64 + sizeof(double) * (size_t)ctiles * 128 * 64;
+}
+
+}  // namespace qrdm

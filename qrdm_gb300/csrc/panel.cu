@@ -21,8 +21,12 @@
 // w_c = C(i,c) + (x.C_c)/(alpha-beta) and applies H(i) to its rows, then
 // computes the partials of column i+1.  At the end each CTA adds its rows'
 // contribution to V^T V (needed by the T factor).
+#include <cooperative_groups.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
+
+namespace cg = cooperative_groups;
 
 namespace qrdm {
 
@@ -213,6 +217,249 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
   if (g == 0 && threadIdx.x == 0) p.st->fjb_cmp = kc;
 }
 
+// ------------------------------------------------ clustered panel (K-panel)
+// Same arithmetic as k_panel, launched as clusters of kPanelCluster CTAs:
+// per column, each CTA's partial slots are summed by its cluster leader
+// through distributed shared memory (fixed order), the leaders publish
+// cluster totals and advance a global counter, every CTA spins (bounded) on
+// that counter and then sums the nclusters totals in a fixed order, so all
+// CTAs hold bit-identical scalars.  The w_c of the reflector application are
+// formed by one thread per column.
+constexpr int kPanelCluster = 8;
+
+__global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* S = reinterpret_cast<double*>(smem_raw);  // [fjb][R]
+  __shared__ PanelSmem sm;
+  __shared__ double s_part[2][QRDM_NB_MAX + 1];
+  cg::cluster_group cl = cg::this_cluster();
+  // cluster shape as launched (the DSMEM reads below only address ranks
+  // that exist, whatever cluster size the kernel actually runs with)
+  const unsigned crank = cl.block_rank();
+  const int csize = (int)cl.num_blocks();
+  const int G = gridDim.x, g = blockIdx.x, R = p.rows_per_cta;
+  const int ncl = G / csize, cid = g / csize;
+  const int fjb = p.st->fjb;
+  const int grow0 = g * R;
+  const int nr = max(0, min(R, p.mloc - grow0));
+  const size_t lda = (size_t)p.lda;
+  double* W0 = p.A + (size_t)p.j * lda + p.j;
+  const int stride = QRDM_NB_MAX + 1;
+  const int tid = threadIdx.x;
+
+  for (int c = tid; c < fjb; c += blockDim.x) sm.sc[c] = pow2_scale_for(p.nrm[c]);
+  if (tid == 0) {
+    sm.exit_flag = 0;
+    sm.thres = 5e-14;
+  }
+  __syncthreads();
+  for (int e = tid; e < fjb * nr; e += blockDim.x) {
+    int c = e / nr, rr = e % nr;
+    S[(size_t)c * R + rr] = W0[(size_t)c * lda + grow0 + rr] * sm.sc[c];
+  }
+  __syncthreads();
+  panel_partials(S, R, nr, grow0, 0, fjb, s_part[0]);
+  if (grow0 <= 0 && 0 < grow0 + nr)
+    for (int c = tid; c < fjb; c += blockDim.x) p.rowbuf[c] = S[(size_t)c * R + (0 - grow0)];
+
+  // Every CTA executes exactly fjb + 1 cluster barriers whatever happens
+  // (early exit, barrier timeout), so no CTA can wait at a cluster barrier
+  // its peers never reach; after an exit or a timeout a CTA only keeps
+  // joining the cluster barriers.
+  int done = fjb;
+  bool ok = true;
+  bool active = true;
+  for (int i = 0; i < fjb; ++i) {
+    const int buf = i & 1;
+    const int nslot = fjb - i;
+    double* part = p.part + (size_t)buf * ncl * stride;
+    const double* rowb = p.rowbuf + (size_t)buf * (QRDM_NB_MAX + 2);
+    cl.sync();
+    if (!active) continue;
+    // 1. cluster: leader sums the member partials (DSMEM, fixed order)
+    if (crank == 0) {
+      for (int sl = tid; sl < nslot; sl += blockDim.x) {
+        double acc = 0.0;
+        for (int r = 0; r < csize; ++r) acc += cl.map_shared_rank(&s_part[buf][0], r)[sl];
+        part[(size_t)cid * stride + sl] = acc;
+      }
+    }
+    // 2. grid: leaders arrive, everyone waits (bounded) for all leaders
+    __syncthreads();
+    if (tid == 0) {
+      if (crank == 0) {
+        __threadfence();
+        red_release_add_u32(p.bar, 1u);
+      }
+      const unsigned target = (unsigned)ncl * (unsigned)(i + 1);
+      unsigned spins = 0;
+      while (ld_acquire_u32(p.bar) < target) {
+        if (++spins > QRDM_SPIN_LIMIT || (*(volatile int*)&p.st->err & QRDM_EDEV_BARRIER_TIMEOUT)) {
+          atomicOr(&p.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+          sm.exit_flag = 2;
+          break;
+        }
+        if (spins > 32) __nanosleep(20);
+      }
+      __threadfence();
+    }
+    __syncthreads();
+    if (sm.exit_flag == 2) {
+      ok = false;
+      active = false;
+      continue;
+    }
+    // 3. fixed-order sum of the cluster totals: 4 threads per slot
+    for (int base = 0; base < nslot; base += 64) {
+      const int sl = base + (tid >> 2), q0 = tid & 3;
+      double acc = 0.0;
+      if (sl < nslot)
+        for (int q = q0; q < ncl; q += 4) acc += __ldcg(part + (size_t)q * stride + sl);
+      acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+      acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+      if (sl < nslot && q0 == 0) sm.red[sl] = acc;
+    }
+    __syncthreads();
+    // 4. dlarfg scalars (thread 0), then w_c in parallel
+    if (tid == 0) {
+      const double sci = sm.sc[i];
+      const double alpha = __ldcg(rowb + i);
+      const int order = p.mloc - i;
+      sm.tau_zero = 1;
+      sm.tau = 0.0;
+      sm.scal = 0.0;
+      sm.beta = alpha;
+      if (order > 1) {
+        double xs = sqrt(sm.red[0]);
+        double xnorm = xs / sci;
+        if (i > 0 && p.allow_exit && xnorm < sm.thres) {
+          sm.exit_flag = 1;
+        } else if (xs != 0.0) {
+          double beta = -sign_of(hypot_lapack(alpha, xs), alpha);
+          sm.tau = (beta - alpha) / beta;
+          sm.scal = 1.0 / (alpha - beta);
+          sm.beta = beta;
+          sm.tau_zero = 0;
+        }
+      }
+      if (!sm.exit_flag) {
+        if (i == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(sm.beta / sci);
+        if (g == 0) p.tau[i] = sm.tau;
+      }
+    }
+    __syncthreads();
+    if (sm.exit_flag == 1) {
+      done = i;
+      active = false;
+      continue;
+    }
+    for (int c = i + 1 + tid; c < fjb; c += blockDim.x) {
+      const double w = __ldcg(rowb + c) + sm.scal * sm.red[c - i];
+      sm.tw[c] = sm.tau * w;
+    }
+    __syncthreads();
+    // 5. apply H(i) to this CTA's rows, then the partials of column i+1
+    if (!sm.tau_zero) {
+      const double scal = sm.scal;
+      const int ncol_r = fjb - i - 1;
+      int rr0 = i + 1 - grow0;
+      if (rr0 < 0) rr0 = 0;
+      double* x = S + (size_t)i * R;
+      for (int rr = rr0 + tid; rr < nr; rr += blockDim.x) x[rr] *= scal;
+      __syncthreads();
+      for (int e = tid; e < ncol_r * nr; e += blockDim.x) {
+        int cc = e / nr, rr = e % nr;
+        int c = i + 1 + cc;
+        int grow = grow0 + rr;
+        if (grow > i) S[(size_t)c * R + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * R + rr]);
+        else if (grow == i) S[(size_t)c * R + rr] -= sm.tw[c];
+      }
+      if (grow0 <= i && i < grow0 + nr && tid == 0) x[i - grow0] = sm.beta;
+    }
+    __syncthreads();
+    if (i + 1 < fjb) {
+      panel_partials(S, R, nr, grow0, i + 1, fjb, s_part[buf ^ 1]);
+      if (grow0 <= i + 1 && i + 1 < grow0 + nr) {
+        double* rb = p.rowbuf + (size_t)(buf ^ 1) * (QRDM_NB_MAX + 2);
+        for (int c = i + 1 + tid; c < fjb; c += blockDim.x) rb[c] = S[(size_t)c * R + (i + 1 - grow0)];
+      }
+    }
+  }
+  // keep every CTA's shared memory alive until the leader's last DSMEM read
+  cl.sync();
+  if (!ok) return;
+  const int kc = done;
+  for (int e = tid; e < fjb * nr; e += blockDim.x) {
+    int c = e / nr, rr = e % nr;
+    int grow = grow0 + rr;
+    double v = S[(size_t)c * R + rr];
+    if (!(c < kc && grow > c)) v = v / sm.sc[c];
+    W0[(size_t)c * lda + grow] = v;
+  }
+  double* vp = p.vtv_part + (size_t)g * QRDM_NB_MAX * QRDM_NB_MAX;
+  int npair = kc * (kc - 1) / 2;
+  for (int t = tid; t < npair; t += blockDim.x) {
+    int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+    while (b * (b - 1) / 2 > t) --b;
+    while ((b + 1) * b / 2 <= t) ++b;
+    int a = t - b * (b - 1) / 2;
+    const double* va = S + (size_t)a * R;
+    const double* vb = S + (size_t)b * R;
+    double acc = 0.0;
+    int rstart = b - grow0;
+    if (rstart < 0) rstart = 0;
+    for (int rr = rstart; rr < nr; ++rr) {
+      int grow = grow0 + rr;
+      double y = (grow == b) ? 1.0 : vb[rr];
+      acc = fma(va[rr], y, acc);
+    }
+    vp[a * QRDM_NB_MAX + b] = acc;
+  }
+  if (g == 0 && tid == 0) p.st->fjb_cmp = kc;
+}
+
+// Launch the clustered panel (cooperative + cluster attributes) on G CTAs
+// (a multiple of kPanelCluster); returns the CUDA error of the launch.
+cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, size_t smem, cudaStream_t s) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(G);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[2];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kPanelCluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  at[1].id = cudaLaunchAttributeCooperative;
+  at[1].val.cooperative = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 2;
+  return cudaLaunchKernelEx(&cfg, k_panel_cluster, pa);
+}
+
+// Largest number of co-resident clusters for the clustered panel with the
+// given dynamic shared memory (0 if the configuration cannot run).
+int panel_cluster_capacity(size_t smem) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(kPanelCluster);
+  cfg.blockDim = dim3(256);
+  cfg.dynamicSmemBytes = smem;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = kPanelCluster;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  int n = 0;
+  if (cudaOccupancyMaxActiveClusters(&n, k_panel_cluster, &cfg) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return n;
+}
+
 // Reset the block record and set the block's column counts (used by the
 // unpivoted QR and the Q application, whose blocks have fixed widths).
 __global__ void k_block_init(BlockState* st, int fjb, int fjb_cmp) {
@@ -271,7 +518,7 @@ __global__ void k_vtv_reduce(const double* __restrict__ vtv_part, int G,
 // T(i,i) = tau_i; T(0:i, i) = -tau_i T(0:i,0:i) (V(:,0:i)^T v_i) (zero when
 // tau_i = 0), from the reduced V^T V.  One CTA; T is built in shared memory
 // (dynamic, kmax^2 doubles) and stored column-major with leading dim ldt.
-__global__ void __launch_bounds__(256) k_larft(const double* __restrict__ vtv,
+__global__ void __launch_bounds__(512) k_larft(const double* __restrict__ vtv,
                                                const double* __restrict__ tau,
                                                const BlockState* __restrict__ st,
                                                double* __restrict__ T, int ldt) {
@@ -281,17 +528,19 @@ __global__ void __launch_bounds__(256) k_larft(const double* __restrict__ vtv,
   const int k = st->fjb_cmp;
   for (int e = threadIdx.x; e < k * k; e += blockDim.x) sT[e] = 0.0;
   __syncthreads();
+  // column i: T(a, i) = sum_{b=a}^{i-1} T(a, b) y_b, y = -tau_i V^T v_i;
+  // 4 threads per output row a (interleaved b), combined by shuffles
+  const int a = threadIdx.x >> 2, part = threadIdx.x & 3;
   for (int i = 0; i < k; ++i) {
     const double ti = tau[i];
     if (threadIdx.x < i) s_y[threadIdx.x] = -ti * vtv[i * (i - 1) / 2 + threadIdx.x];
     __syncthreads();
-    if (threadIdx.x < i) {
-      int a = threadIdx.x;
-      double acc = 0.0;
-      if (ti != 0.0)
-        for (int b = a; b < i; ++b) acc = fma(sT[b * k + a], s_y[b], acc);
-      sT[i * k + a] = acc;
-    }
+    double acc = 0.0;
+    if (a < i && ti != 0.0)
+      for (int b = a + part; b < i; b += 4) acc = fma(sT[b * k + a], s_y[b], acc);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    if (a < i && part == 0) sT[i * k + a] = acc;
     if (threadIdx.x == 0) sT[i * k + i] = ti;
     __syncthreads();
   }

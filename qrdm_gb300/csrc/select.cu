@@ -17,8 +17,11 @@
 //            into a position permutation (dst <- src).
 //   K-swap   k_permute_columns: applies that permutation to whole columns of
 //            A (all m rows), staged through shared memory, coalesced.
+#include <cuda_bf16.h>
+
 #include "common.cuh"
 #include "kernels.cuh"
+#include "tc.cuh"
 
 namespace qrdm {
 
@@ -48,7 +51,6 @@ __device__ void bitonic_sort(Cand* s) {
 }
 
 constexpr int TOPK_TILE = kTopkTile;
-constexpr int TOPK_FINAL = kTopkFinal;
 
 // Each CTA sorts TOPK_TILE entries and keeps its first kmax.
 // Source: either nrm[col0 + i] (in_cand == nullptr) or in_cand[i].
@@ -80,16 +82,24 @@ __global__ void __launch_bounds__(1024) k_topk_tile(const double* __restrict__ n
   for (int t = threadIdx.x; t < kmax; t += blockDim.x) out[blockIdx.x * kmax + t] = s[t];
 }
 
-// Final sort of <= TOPK_FINAL entries; writes the kmax best and nc.
-__global__ void __launch_bounds__(1024) k_topk_final(const Cand* __restrict__ in_cand, int count,
+// Final sort of <= N entries (N a power of two >= count); writes the kmax
+// best and nc.  Source: in_cand[0..count) or, when in_cand is null, the
+// partial norms nrm[0..count) with their positions as indices.
+template <int N>
+__global__ void __launch_bounds__(1024) k_topk_final(const Cand* __restrict__ in_cand,
+                                                     const double* __restrict__ nrm, int count,
                                                      int kmax, double tau_rel,
                                                      Cand* __restrict__ cand, BlockState* st) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  Cand* s = reinterpret_cast<Cand*>(smem_raw);
-  for (int t = threadIdx.x; t < TOPK_FINAL; t += blockDim.x) {
+  __shared__ Cand s[N];
+  for (int t = threadIdx.x; t < N; t += blockDim.x) {
     Cand c;
     if (t < count) {
-      c = in_cand[t];
+      if (in_cand) {
+        c = in_cand[t];
+      } else {
+        c.val = nrm[t];
+        c.idx = t;
+      }
     } else {
       c.val = -1.0;
       c.idx = 0x7fffffff;
@@ -98,14 +108,34 @@ __global__ void __launch_bounds__(1024) k_topk_final(const Cand* __restrict__ in
     s[t] = c;
   }
   __syncthreads();
-  bitonic_sort<TOPK_FINAL>(s);
-  for (int t = threadIdx.x; t < kmax; t += blockDim.x) cand[t] = s[t];
+  bitonic_sort<N>(s);
+  for (int t = threadIdx.x; t < kmax; t += blockDim.x) cand[t] = t < N ? s[t] : Cand{-1.0, 0x7fffffff, 0};
   if (threadIdx.x == 0) {
     double cut = tau_rel * s[0].val;
     int nc = 0;
-    while (nc < count && nc < kmax && s[nc].val > cut) ++nc;
+    while (nc < count && nc < kmax && nc < N && s[nc].val > cut) ++nc;
     st->nc = nc;
   }
+}
+
+void launch_topk_final(int count, cudaStream_t st_, const Cand* in_cand, const double* nrm, int kmax,
+                       double tau_rel, Cand* cand, BlockState* st) {
+  int n = 64;
+  while (n < count) n <<= 1;
+  const int threads = n >= 2048 ? 1024 : (n / 2 < 32 ? 32 : n / 2);
+#define TOPK_CASE(N) \
+  case N: k_topk_final<N><<<1, threads, 0, st_>>>(in_cand, nrm, count, kmax, tau_rel, cand, st); break;
+  switch (n) {
+    TOPK_CASE(64)
+    TOPK_CASE(128)
+    TOPK_CASE(256)
+    TOPK_CASE(512)
+    TOPK_CASE(1024)
+    TOPK_CASE(2048)
+    default:
+      k_topk_final<4096><<<1, 1024, 0, st_>>>(in_cand, nrm, count, kmax, tau_rel, cand, st);
+  }
+#undef TOPK_CASE
 }
 
 // Partial cosine matrix over rows [r_begin, r_end) of the window:
@@ -208,25 +238,40 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   unsigned* bits = reinterpret_cast<unsigned*>(s_swb + maxsw);
   __shared__ int s_nsel, s_nswap;
   int nwords = (ncols + 31) >> 5;
+  double* s_g = reinterpret_cast<double*>(bits + ((nwords + 3) & ~3));  // [nc][nc] cosines
+  const int nc = st->nc;
   for (int w = threadIdx.x; w < nwords; w += blockDim.x) bits[w] = 0u;
+  for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) s_g[e] = gram[(size_t)(e / nc) * km + (e % nc)];
   __syncthreads();
-  if (threadIdx.x == 0) {
-    int nc = st->nc;
+  // greedy in norm order (warp 0): candidate i is taken iff every |cos| with
+  // the columns taken so far is < delta; the max over taken columns is a
+  // warp reduction
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
     int nsel = 1;
-    s_sel[0] = cand[0].idx;
-    s_pos[0] = 0;
+    if (lane == 0) {
+      s_sel[0] = cand[0].idx;
+      s_pos[0] = 0;
+    }
+    __syncwarp();
     for (int i = 1; i < nc; ++i) {
       double worst = 0.0;
-      for (int s = 0; s < nsel; ++s) {
-        double c = fabs(gram[(size_t)s_pos[s] * km + i]);
-        if (worst < c) worst = c;
-      }
+      for (int q = lane; q < nsel; q += 32) worst = fmax(worst, fabs(s_g[s_pos[q] * nc + i]));
+      worst = warp_max(worst);
       if (worst < delta && nsel < kmax) {
-        s_pos[nsel] = i;
-        s_sel[nsel] = cand[i].idx;
+        if (lane == 0) {
+          s_pos[nsel] = i;
+          s_sel[nsel] = cand[i].idx;
+        }
         ++nsel;
       }
+      __syncwarp();
     }
+    if (lane == 0) s_nsel = nsel;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int nsel = s_nsel;
     for (int s = 0; s < nsel; ++s) bits[s_sel[s] >> 5] |= 1u << (s_sel[s] & 31);
 #define MARK(p) ((bits[(p) >> 5] >> ((p) & 31)) & 1u)
 #define XCHG(p, q)                                                        \
@@ -367,4 +412,129 @@ void launch_gram_partial(int km, int nchunk, cudaStream_t s, const double* A, lo
     k_gram_partial<128><<<nchunk, 256, 0, s>>>(A, lda, j, mloc, rows_per_chunk, cand, st, part);
 }
 
+// ---------------------------------------------- mixed-precision cosines
+// K-gram (mixed): the candidate cosines in BF16 on tcgen05 with FP32
+// accumulation, then an FP64 recheck of every cosine whose BF16 value lies
+// within `margin` of delta.  The scaled candidate columns (|entries| with
+// column norm ~1) are rounded to BF16 (relative 2^-9 each), so a computed
+// cosine is within 2^-8 of the exact one; the default margin is 2^-7.
+// One CTA per row chunk: the candidates fill rows p < nc of one 128 x 64
+// K-major tile per 64-row block (rows >= nc zero); the same tile's first 64
+// rows serve as the N operand, D = 128 x 64 in TMEM (FP32), of which the
+// first nc x nc block is written out (as FP64 partials, summed by
+// k_gram_reduce in a fixed order).
+
+__global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A, long long lda, int j,
+                                                   int mloc, int rows_per_chunk,
+                                                   const Cand* __restrict__ cand,
+                                                   BlockState* __restrict__ st, double* __restrict__ part) {
+  __shared__ __align__(1024) unsigned char tile[128 * 128];
+  __shared__ double s_rc[64];
+  __shared__ int s_col[64];
+  __shared__ uint64_t bar;
+  __shared__ uint32_t s_tmem;
+  const int nc = st->nc;
+  if (nc <= 1) return;
+  const int tid = threadIdx.x;
+  const int r_begin = blockIdx.x * rows_per_chunk;
+  const int r_end = min(mloc, r_begin + rows_per_chunk);
+  if (tid < 64) {
+    s_rc[tid] = tid < nc ? 1.0 / cand[tid].val : 0.0;
+    s_col[tid] = tid < nc ? j + cand[tid].idx : 0;
+  }
+  // rows >= 64 of the tile stay zero for the whole kernel
+  for (int e = tid; e < 128 * 128 / 16; e += blockDim.x) reinterpret_cast<uint4*>(tile)[e] = make_uint4(0, 0, 0, 0);
+  if (tid == 0) {
+    tc::mbar_init(&bar, 1);
+    tc::fence_mbar_init();
+  }
+  if (tid < 32) tc::tmem_alloc(&s_tmem, 64);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  uint32_t phase = 0;
+  bool ok = true, first = true;
+  for (int r0 = r_begin; r0 < r_end && ok; r0 += 64) {
+    // candidate p, rows r0..r0+63 (pairs of rows per thread store)
+    for (int e = tid; e < 64 * 32; e += blockDim.x) {
+      const int p = e >> 5, kp = e & 31;
+      const int r = r0 + 2 * kp;
+      float v0 = 0.f, v1 = 0.f;
+      if (p < nc) {
+        const double* col = A + (size_t)s_col[p] * lda + j;
+        if (r < r_end) v0 = (float)(s_rc[p] * col[r]);
+        if (r + 1 < r_end) v1 = (float)(s_rc[p] * col[r + 1]);
+      }
+      __nv_bfloat162 b2 = __floats2bfloat162_rn(v0, v1);
+      *reinterpret_cast<__nv_bfloat162*>(tile + tc::sw128_offset(p, 2 * kp)) = b2;
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
+      for (int kk = 0; kk < 4; ++kk) {
+        const uint64_t d = tc::desc_sw128(tc::smem_u32(tile) + kk * 32);
+        tc::mma_bf16(tmem, d, d, idesc, (first && kk == 0) ? 0u : 1u);
+      }
+      tc::mma_commit(&bar);
+    }
+    first = false;
+    if (!tc::mbar_wait(&bar, phase)) {
+      atomicOr(&st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+      ok = false;
+    }
+    phase ^= 1u;
+    tc::fence_after_sync();
+    __syncthreads();
+  }
+  // lanes 0..63 hold rows p = 0..63 (warps 0 and 1)
+  const int w = tid >> 5, lane = tid & 31;
+  if (w < 2 && !first && ok) {
+    const int p = 32 * w + lane;
+    for (int c0 = 0; c0 < 64; c0 += 16) {
+      float v[16];
+      tc::tmem_ld16(tmem + ((uint32_t)(32 * w) << 16) + c0, v);
+      tc::tmem_wait_ld();
+      for (int i = 0; i < 16; ++i) part[(size_t)blockIdx.x * 64 * 64 + p * 64 + c0 + i] = (double)v[i];
+    }
+  } else if (w < 2 && first) {  // empty chunk: zero partial
+    const int p = 32 * w + lane;
+    for (int q = 0; q < 64; ++q) part[(size_t)blockIdx.x * 64 * 64 + p * 64 + q] = 0.0;
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (tid < 32) tc::tmem_dealloc(tmem, 64);
+}
+
+// FP64 recheck of the cosines within margin of delta: one warp per pair
+// (p < q < nc); the exact dot of the two scaled candidate columns replaces
+// both symmetric entries.
+__global__ void __launch_bounds__(256) k_gram_recheck(const double* __restrict__ A, long long lda, int j,
+                                                      int mloc, const Cand* __restrict__ cand,
+                                                      double delta, double margin, int km,
+                                                      BlockState* __restrict__ st, double* __restrict__ gram) {
+  const int nc = st->nc;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+  const int npair = nc * (nc - 1) / 2;
+  if (warp >= npair) return;
+  int q = (int)((1.0 + sqrt(1.0 + 8.0 * (double)warp)) * 0.5);
+  while (q * (q - 1) / 2 > warp) --q;
+  while ((q + 1) * q / 2 <= warp) ++q;
+  const int p = warp - q * (q - 1) / 2;
+  const double g = gram[(size_t)p * km + q];
+  if (!(fabs(fabs(g) - delta) < margin)) return;
+  const double rp = 1.0 / cand[p].val, rq = 1.0 / cand[q].val;
+  const double* cp = A + (size_t)(j + cand[p].idx) * lda + j;
+  const double* cq = A + (size_t)(j + cand[q].idx) * lda + j;
+  double acc = 0.0;
+  for (int r = lane; r < mloc; r += 32) acc = fma(rp * cp[r], rq * cq[r], acc);
+  acc = warp_sum(acc);
+  if (lane == 0) {
+    gram[(size_t)p * km + q] = acc;
+    gram[(size_t)q * km + p] = acc;
+    atomicAdd(&st->rechecks, 1);
+  }
+}
 }  // namespace qrdm
