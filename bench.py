@@ -1,15 +1,22 @@
 """Benchmark of the GB300 DM-QR hot path.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
-                    [--workload lowrank16k|gauss4k|kahan4k|graded1k]
+                    [--workload lowrank16k|gauss4k|kahan4k|graded1k|batched2000]
                     [--precision mixed|fp64] [--no-variants]
 
 One step = one DM-QR factorisation of the workload matrix, already resident
 in HBM (restored from a pristine device copy before each step; the copy is
 inside the timed region).  The default workload is the 16384 x 8192
 numerical-rank-2048 matrix A = L R^T + 1e-10 E (full factorisation, nb = 64,
-delta = 0.9, tau_ = 0.15).  Inputs (1.07 GB) are larger than the 129 MB L2,
-so no explicit flush is needed between steps.
+delta = 0.9, tau_ = 0.15) in the mixed-precision form (Ozaki-split BF16
+trailing update, BF16 cosine Gram with FP64 recheck).  Inputs (1.07 GB) are
+larger than the 129 MB L2, so no explicit flush is needed between steps.
+
+--workload batched2000: one step = the batched DM-QR of 2000 uneven
+matrices (n log-uniform in [32, 512], m = n r, r log-uniform in [1, 4],
+capped at 2048; U diag(s) V^T with geometric decay to 10^-d, d ~ U[4, 14])
+in one persistent launch; value = matrices/s; the roofline is the summed
+per-problem bound sum_i max(F_i / P_fp64, 16 m_i n_i / BW).
 
 value = effective FP64 TFLOP/s = F / t with F = 2 m n^2 - 2 n^3 / 3 (whole job
 over all ranks; ranks run independent replicas).  e2e = the same metric
@@ -42,7 +49,11 @@ WORKLOADS = {
     "gauss4k": (4096, 4096, "i.i.d. N(0,1)"),
     "kahan4k": (4096, 4096, "Kahan c=0.285 + 1e-14 N(0,1)"),
     "graded1k": (1000, 1000, "U diag(10^(-12(i-1)/999)) V^T"),
+    "batched2000": (0, 0, "2000 uneven U diag(s) V^T, n in [32, 512], m = n r, r in [1, 4]"),
 }
+BATCH_COUNT, BATCH_NB = 2000, 32
+BATCH_CPU_SAMPLE = 400
+FP64_PEAK_TFLOPS = 1.25  # nominal dense FP64 of GB300 (no measured FP64 peak)
 NB, DELTA, TAU_ = 64, 0.9, 0.15
 CPU_SAMPLE_K = 2048
 
@@ -317,10 +328,21 @@ def run_ours(args):
                     "traffic": load_traffic("trail_fp64"),
                     "per_launch_basis": f"4 m' n' k flops per DM block, {nblk} blocks"}
         else:
-            achieved = sti.trail_flops / (sti.ms_trail / 1e3) / 1e12
-            roof = {"bound": "tensor", "kernel": "Ozaki trailing update", "achieved": achieved,
-                    "peak": peaks.get("bf16_tflops"), "peak_kind": peak_kind,
-                    "unit": "TFLOP/s", "frac": None, "traffic": load_traffic("trail_ozaki")}
+            # Ozaki split: s digits per operand, the s (s + 1) / 2 digit
+            # products of level <= s + 1 are BF16 GEMMs of the FP64 shape
+            s_dig = int(default_options().slices) or 7
+            prods = s_dig * (s_dig + 1) // 2
+            tflop = sti.trail_flops * prods
+            achieved = tflop / (sti.ms_trail / 1e3) / 1e12
+            peak = peaks.get("bf16_tflops_sustained")
+            roof = {"bound": "tensor", "kernel": "Ozaki trailing update (k_oz_slice_v, "
+                    "k_oz_gemm1, k_oz_w2, k_oz_gemm2), BF16 tcgen05", "achieved": achieved,
+                    "peak": peak, "peak_kind": f"{peak_kind} bf16 sustained (the phase runs "
+                    "inside a long step)", "unit": "TFLOP/s", "frac": achieved / peak,
+                    "traffic": load_traffic("trail_ozaki"),
+                    "per_launch_basis": f"{prods} BF16 digit products x 4 m' n' k flops per DM "
+                                        f"block, {nblk} blocks",
+                    "fp64_equivalent_tflops": sti.trail_flops / (sti.ms_trail / 1e3) / 1e12}
         # e2e through the host C ABI with pinned host buffers
         a_host = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
         a_host.copy_(pristine)
@@ -348,9 +370,27 @@ def run_ours(args):
         variants = {}
         if args.variants:
             if prec != 0:
-                st64, _ = step(precision=0)
+                st64 = Stats()
+                st64.timing = 1
+                step(st64, precision=0)
                 variants["fp64_dmqr_ms"] = st64.ms_total
                 variants["fp64_dmqr_tflops"] = F / (st64.ms_total / 1e3) / 1e12
+            # GPU QP3 (dgeqp3 semantics) on the same matrix, one run
+            work.copy_(pristine)
+            jp.zero_()
+            q0 = torch.cuda.Event(enable_timing=True)
+            q1 = torch.cuda.Event(enable_timing=True)
+            q0.record(stream)
+            rq = L.dgeqp3_dev(102, m, n, C.c_void_p(work.data_ptr()), m,
+                              C.c_void_p(jp.data_ptr()), C.c_void_p(tau.data_ptr()))
+            q1.record(stream)
+            torch.cuda.synchronize()
+            if rq == 0:
+                variants["qp3_ms"] = q0.elapsed_time(q1)
+                variants["qp3_tflops"] = F / (variants["qp3_ms"] / 1e3) / 1e12
+                variants["speedup_vs_qp3"] = variants["qp3_ms"] / ms
+            if "fp64_dmqr_ms" in variants:
+                variants["speedup_vs_fp64"] = variants["fp64_dmqr_ms"] / ms
             variants["phase_ms"] = phase
             variants["blocks"] = nblk
         cpu = None
@@ -380,6 +420,230 @@ def run_ours(args):
     return out
 
 
+# ------------------------------------------------------------------ batched
+def batched_problem_device(i, m, n, seed=4):
+    """Matrix i of the batched workload on the GPU (torch, seeded): U (m x n)
+    and V (n x n) orthonormal from Gaussians, s geometric from 1 to 10^-d,
+    d ~ U[4, 14].  Returned column-major as a flat float64 tensor."""
+    import torch
+
+    g = torch.Generator(device="cuda").manual_seed(seed * 1000003 + i)
+    d = 4.0 + 10.0 * torch.rand(1, generator=g, dtype=torch.float64, device="cuda")
+    u, _ = torch.linalg.qr(torch.randn(m, n, generator=g, dtype=torch.float64, device="cuda"))
+    v, _ = torch.linalg.qr(torch.randn(n, n, generator=g, dtype=torch.float64, device="cuda"))
+    k = torch.arange(n, dtype=torch.float64, device="cuda")
+    s = torch.pow(10.0, -d * k / max(n - 1, 1))
+    a = (u * s) @ v.T
+    return a.T.contiguous().view(-1)
+
+
+def batched_setup(seed=4):
+    import torch
+
+    from qrdm_gb300 import BatchedDMQR
+    from qrdm_gb300.workloads import batched_shapes
+
+    ms, ns = batched_shapes(BATCH_COUNT, seed=seed)
+    shapes = [(int(m), int(n)) for m, n in zip(ms, ns)]
+    b = BatchedDMQR(shapes)
+    for i, (m, n) in enumerate(shapes):
+        b.a[b.a_off[i]:b.a_off[i + 1]] = batched_problem_device(i, m, n, seed)
+    torch.cuda.synchronize()
+    return b, shapes
+
+
+def batched_roofline_s(shapes, bw_gbs):
+    """Summed roofline time: each problem at max(flops / FP64 peak, bytes / BW)."""
+    t = 0.0
+    for m, n in shapes:
+        t += max(flops_full(m, n) / (FP64_PEAK_TFLOPS * 1e12), 16.0 * m * n / (bw_gbs * 1e9))
+    return t
+
+
+def batched_errors(b, pristine):
+    """Per-problem backward error ||A P - Q R||_F / ||A||_F and orthogonality
+    ||I - Q^T Q||_F on the GPU (torch Householder product of the factors)."""
+    import torch
+
+    a_out = b.a
+    jp = b.jpvt.cpu().numpy()
+    be, orth = [], []
+    for i, (m, n) in enumerate(b.shapes):
+        k = min(m, n)
+        A0 = pristine[b.a_off[i]:b.a_off[i + 1]].view(n, m).T
+        F = a_out[b.a_off[i]:b.a_off[i + 1]].view(n, m).T
+        tau = b.tau[b.t_off[i]:b.t_off[i] + k]
+        Q = torch.linalg.householder_product(F[:, :k], tau)
+        R = torch.triu(F[:k, :])
+        perm = torch.from_numpy(jp[b.v_off[i]:b.v_off[i + 1]].astype(np.int64) - 1).cuda()
+        AP = A0[:, perm]
+        be.append(float(torch.linalg.norm(AP - Q @ R) / torch.linalg.norm(A0)))
+        orth.append(float(torch.linalg.norm(torch.eye(k, dtype=torch.float64, device="cuda") - Q.T @ Q)))
+    return np.array(be), np.array(orth)
+
+
+def batched_cpu_sample(b_shapes, pristine_host, offs, threads, seed=7):
+    """Oracle DM-QR over a seeded random sample of the batch's problems."""
+    from oracle.oracle import Oracle, run_dmqr
+
+    rng = np.random.default_rng(seed)
+    idx = rng.choice(len(b_shapes), size=min(BATCH_CPU_SAMPLE, len(b_shapes)), replace=False)
+    o = Oracle(threads=threads)
+    mats = []
+    for i in idx:
+        m, n = b_shapes[i]
+        mats.append(pristine_host[offs[i]:offs[i + 1]].reshape(n, m).T)
+    t0 = time.perf_counter()
+    for A0 in mats:
+        r = run_dmqr(o, A0, nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+        assert r["info"] == 0
+    dt = time.perf_counter() - t0
+    return {"value": len(mats) / dt, "seconds": dt, "problems": len(mats)}
+
+
+def run_batched(args):
+    import torch
+
+    from qrdm_gb300 import lib
+
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    L = lib()
+    stream = torch.cuda.current_stream()
+    L.qrdm_set_stream(C.c_void_p(stream.cuda_stream))
+    b, shapes = batched_setup()
+    pristine = b.a.clone()
+    launches_per_step = 1
+
+    def step():
+        b.a.copy_(pristine)
+        r = b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+        if r != 0:
+            raise RuntimeError(f"dgeqrdm_batched_dev returned {r}")
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    barrier(world)
+    with ClockSampler(local) as clk:
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        barrier(world)
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world)
+    value = world * BATCH_COUNT / (ms / 1e3)
+    clocks = clk.summary()
+    if rank == 0:
+        peaks, peak_kind = load_peaks()
+        F = sum(flops_full(m, n) for m, n in shapes)
+        t_roof = batched_roofline_s(shapes, peaks["hbm_gbs"])
+        # kernel-only time of the persistent launch (events around the run)
+        b.a.copy_(pristine)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        kms = e0.elapsed_time(e1)
+        be, orth = batched_errors(b, pristine)
+        achieved = F / (kms / 1e3) / 1e12
+        roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch)",
+                "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
+                "peak_kind": "nominal FP64 (no measured FP64 peak); HBM term from measured "
+                             f"{peaks['hbm_gbs']} GB/s", "unit": "TFLOP/s",
+                "frac": t_roof / (kms / 1e3),
+                "summed_roofline_mats_per_s": BATCH_COUNT / t_roof,
+                "traffic": load_traffic("dmqr_batched"),
+                "per_launch_basis": "sum_i 2 m_i n_i^2 - 2 n_i^3 / 3 flops over 2000 problems"}
+        # e2e: pinned host buffer -> device, factor, factors back to the host
+        host = torch.empty(pristine.numel(), dtype=torch.float64, pin_memory=True)
+        host.copy_(pristine)
+        back = torch.empty_like(host)
+        e2e_t = []
+        for _ in range(2):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            b.a.copy_(host, non_blocking=True)
+            b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+            back.copy_(b.a, non_blocking=True)
+            jp_h = b.jpvt.cpu()
+            tau_h = b.tau.cpu()
+            torch.cuda.synchronize()
+            e2e_t.append(time.perf_counter() - t0)
+        h2d = 8 * pristine.numel()
+        d2h = 8 * pristine.numel() + 4 * b.jpvt.numel() + 8 * b.tau.numel()
+        e2e = {"value": world * BATCH_COUNT / min(e2e_t), "unit": "matrices/s",
+               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+        cpu = None
+        if args.cpu_baseline:
+            threads = os.cpu_count() or 1
+            s = batched_cpu_sample(shapes, pristine.cpu().numpy(), b.a_off, threads)
+            cpu = {"value": s["value"], "unit": "matrices/s", "cores": threads, "kind": "port",
+                   "sample": f"{s['problems']} problems of the batch drawn by seed, factored one "
+                             f"after another by the oracle port on OpenBLAS ({s['seconds']:.1f} s)"}
+        out = {"metric": "batched DM-QR matrices/s", "value": value, "unit": "matrices/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+               "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+               "data": "synthetic",
+               "config": {"workload": "batched2000", "count": BATCH_COUNT, "nb": BATCH_NB,
+                          "delta": DELTA, "tau_": TAU_, "flops": F,
+                          "bytes": 8 * pristine.numel(),
+                          "parallelism": f"replicas{world}",
+                          "l2": "inputs (3.3 GB) larger than L2; no flush needed"},
+               "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
+               "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+               "errors": {"backward_p50": float(np.percentile(be, 50)),
+                          "backward_p99": float(np.percentile(be, 99)),
+                          "backward_max": float(be.max()),
+                          "orth_p50": float(np.percentile(orth, 50)),
+                          "orth_p99": float(np.percentile(orth, 99)),
+                          "kernel_ms": kms}}
+        print(json.dumps(out), flush=True)
+    barrier(world)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+def run_batched_reference(args):
+    import torch
+
+    rank, world, _ = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    b, shapes = batched_setup()
+    host = b.a.cpu().numpy()
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        batched_cpu_sample(shapes, host, b.a_off, threads)
+    vals, secs = [], []
+    for _ in range(args.steps):
+        s = batched_cpu_sample(shapes, host, b.a_off, threads)
+        vals.append(s["value"])
+        secs.append(s["seconds"])
+    v = statistics.median(vals)
+    sample = (f"{s['problems']} problems of the 2000-matrix batch drawn by seed, oracle port of "
+              "the reference on OpenBLAS, one after another")
+    print(json.dumps({
+        "impl": "reference", "metric": "batched DM-QR matrices/s", "value": v,
+        "unit": "matrices/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": statistics.median(secs) * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batched2000", "count": BATCH_COUNT, "nb": BATCH_NB},
+        "cpu_baseline": {"value": v, "unit": "matrices/s", "cores": threads, "kind": "port",
+                         "sample": sample},
+        "e2e": {"value": v, "unit": "matrices/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0}}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -387,11 +651,16 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="lowrank16k")
-    ap.add_argument("--precision", choices=["mixed", "fp64"], default="fp64")
+    ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
-    if args.impl == "reference":
+    if args.workload == "batched2000":
+        if args.impl == "reference":
+            run_batched_reference(args)
+        else:
+            run_batched(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -109,6 +109,22 @@ int dgeqrdm_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jp
 int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt,
                         double* d_tau, int* ncols, const double* thres, int nb, void* stream);
 
+/* ------------------------------------------------------------- batched */
+/* `count` independent DM-QR problems of uneven size in one persistent
+ * kernel (one CTA per problem, largest first), FP64.  No counterpart in the
+ * reference (it factors one matrix per call); each problem follows dgeqrdm
+ * exactly, with jpvt treated as all-free.  m, n: host arrays of count ints
+ * (1 <= n <= 1024); device buffers packed in problem order:
+ *   d_a     sum m_i n_i doubles, problem i column-major with lda = m_i
+ *   d_jpvt  sum n_i ints (out), d_ncols sum n_i ints (out: DM block sizes,
+ *           zero after the last block), d_tau sum min(m_i, n_i) doubles,
+ *           d_info count ints (0 or -13) or NULL.
+ * thres = [delta, tau_, eta] (host), stop = the stop mode of dgeqrdm's
+ * ncols[0] (0..3) for every problem, nb <= 64.  Repeated calls with the same
+ * description replay a captured CUDA graph. */
+int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int* d_jpvt, double* d_tau,
+                        int* d_ncols, int* d_info, const double* thres, int stop, int nb);
+
 /* ------------------------------------------------------------------ QP3 */
 /* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot
  * per column by largest partial norm, first index on ties; jpvt[j] != 0

@@ -170,11 +170,15 @@ static void note_u(int k, double dist, double unc) {
   if (g_block && v < g_block[g_blk]) g_block[g_blk] = v;
 }
 /* relative uncertainty of a downdated partial norm w whose last exact value
- * was wl: rounding amplified by (wl/w)^2 since then */
+ * was wl.  Two sources: its own rounding, amplified by (wl/w)^2 since then
+ * (each downdate w' = w sqrt(1 - (|r|/w)^2) scales a relative error by
+ * (w/w')^2), and the absolute noise of the new R entries r it subtracts
+ * (w' dw' = |r| dr with |r| up to wl), which gives noise * (wl/w) / w. */
 static double rel_unc(double w, double wl) {
   if (!(w > 0)) return g_eps;
   double r = wl / w;
-  return g_eps * (1.0 + r * r);
+  if (r < 1.0) r = 1.0;
+  return g_eps * (1.0 + r * r) + g_noise * r / w;
 }
 static void note(int k, double v) {
   v /= g_noise;

@@ -62,4 +62,84 @@ def dgeqrdm_device(a, jpvt, tau, nb: int = 64, delta: float = 0.9, tau_: float =
     return {"ncols": nc, "info": int(info), "stats": st.as_dict()}
 
 
-__all__ = ["dgeqrdm", "dgeqrdm_device", "Options", "Stats", "default_options", "lib", "PREC"]
+class BatchedDMQR:
+    """Device-resident batch of uneven DM-QR problems for
+    ``dgeqrdm_batched_dev``: matrices packed column-major in one float64
+    CUDA buffer (problem i at ``a_off[i]`` with lda = m_i), jpvt / ncols at
+    ``v_off[i]``, tau at ``t_off[i]``.  ``load`` copies host matrices in,
+    ``run`` factors all of them with one persistent kernel launch (replayed
+    from a CUDA graph when the description repeats), ``result(i)`` reads one
+    problem back."""
+
+    def __init__(self, shapes, device="cuda"):
+        import torch
+        self.shapes = [(int(m), int(n)) for m, n in shapes]
+        self.count = len(self.shapes)
+        self.m = np.array([s[0] for s in self.shapes], np.int32)
+        self.n = np.array([s[1] for s in self.shapes], np.int32)
+        mn = self.m.astype(np.int64) * self.n
+        self.a_off = np.concatenate([[0], np.cumsum(mn)]).astype(np.int64)
+        self.v_off = np.concatenate([[0], np.cumsum(self.n)]).astype(np.int64)
+        self.t_off = np.concatenate([[0], np.cumsum(np.minimum(self.m, self.n))]).astype(np.int64)
+        self.a = torch.zeros(int(self.a_off[-1]), dtype=torch.float64, device=device)
+        self.jpvt = torch.zeros(int(self.v_off[-1]), dtype=torch.int32, device=device)
+        self.ncols = torch.zeros(int(self.v_off[-1]), dtype=torch.int32, device=device)
+        self.tau = torch.zeros(max(1, int(self.t_off[-1])), dtype=torch.float64, device=device)
+        self.info = torch.zeros(max(1, self.count), dtype=torch.int32, device=device)
+
+    def pack(self, mats) -> np.ndarray:
+        """Host array holding the matrices in the device layout."""
+        buf = np.empty(int(self.a_off[-1]), np.float64)
+        for i, A in enumerate(mats):
+            m, n = self.shapes[i]
+            buf[self.a_off[i]:self.a_off[i + 1]] = np.asarray(A, np.float64).reshape(m, n).ravel(order="F")
+        return buf
+
+    def load(self, mats):
+        import torch
+        self.a.copy_(torch.from_numpy(self.pack(mats)))
+
+    def run(self, nb: int = 32, delta: float = 0.9, tau_: float = 0.15, stop: int = 0,
+            eta: float | None = None) -> int:
+        thres = np.array([delta, tau_, 0.0 if eta is None else eta], np.float64)
+        return int(lib().dgeqrdm_batched_dev(
+            self.count, self.m.ctypes.data_as(C.POINTER(C.c_int)),
+            self.n.ctypes.data_as(C.POINTER(C.c_int)), C.c_void_p(self.a.data_ptr()),
+            C.c_void_p(self.jpvt.data_ptr()), C.c_void_p(self.tau.data_ptr()),
+            C.c_void_p(self.ncols.data_ptr()), C.c_void_p(self.info.data_ptr()),
+            thres.ctypes.data_as(C.POINTER(C.c_double)), int(stop), int(nb)))
+
+    def results(self) -> list:
+        a = self.a.cpu().numpy()
+        jp = self.jpvt.cpu().numpy()
+        nc = self.ncols.cpu().numpy()
+        tau = self.tau.cpu().numpy()
+        info = self.info.cpu().numpy()
+        out = []
+        for i, (m, n) in enumerate(self.shapes):
+            blocks = nc[self.v_off[i]:self.v_off[i + 1]]
+            out.append({
+                "A": a[self.a_off[i]:self.a_off[i + 1]].reshape(n, m).T.copy(),
+                "jpvt": jp[self.v_off[i]:self.v_off[i + 1]].copy(),
+                "ncols": blocks.copy(),
+                "nblocks": int(np.count_nonzero(blocks)),
+                "tau": tau[self.t_off[i]:self.t_off[i + 1]].copy(),
+                "info": int(info[i]),
+            })
+        return out
+
+
+def dgeqrdm_batched(mats, nb: int = 32, delta: float = 0.9, tau_: float = 0.15, stop: int = 0,
+                    eta: float | None = None) -> list:
+    """Factor a list of host matrices (uneven shapes, n <= 1024) with one
+    batched DM-QR launch; returns one result dict per matrix."""
+    mats = [np.asarray(A, np.float64) for A in mats]
+    b = BatchedDMQR([A.shape for A in mats])
+    b.load(mats)
+    r = b.run(nb=nb, delta=delta, tau_=tau_, stop=stop, eta=eta)
+    if r != 0:
+        raise RuntimeError(f"dgeqrdm_batched_dev failed: {r}")
+    return b.results()
+
+
+__all__ = ["dgeqrdm", "dgeqrdm_device", "dgeqrdm_batched", "BatchedDMQR", "Options", "Stats", "default_options", "lib", "PREC"]

@@ -69,6 +69,7 @@ int set_kernel_attributes(int big) {
     CK(cudaFuncSetAttribute(k_trail_w_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_qp3_gemv, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536));
     if (oz_set_attributes()) return QRDM_ERR_CUDA;
+    if (batched_set_attributes()) return QRDM_ERR_CUDA;
   }
   return 0;
 }
@@ -1000,6 +1001,138 @@ int dgeqp3(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, doubl
   return 0;
 }
 
+// ------------------------------------------------------------ batched
+static unsigned long long fnv1a(unsigned long long h, const void* p, size_t n) {
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  for (size_t i = 0; i < n; ++i) {
+    h ^= b[i];
+    h *= 1099511628211ull;
+  }
+  return h;
+}
+
+int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int* d_jpvt, double* d_tau,
+                        int* d_ncols, int* d_info, const double* thres, int stop, int nb) {
+  if (count < 0 || !m || !n || !thres || stop < 0 || stop > 3) return -1;
+  if (count == 0) return 0;
+  const double delta = thres[0], tau_ = thres[1];
+  if (delta < 0.0 || delta > 1.0 || tau_ < 0.0 || tau_ > 1.0 || nb <= 0) return -1;
+  if (nb > batched_kmax()) return QRDM_ERR_UNSUPPORTED;
+  int nmax = 1;
+  for (int i = 0; i < count; ++i) {
+    if (m[i] <= 0 || n[i] <= 0) return -1;
+    if (n[i] > batched_nmax()) return QRDM_ERR_UNSUPPORTED;
+    nmax = std::max(nmax, n[i]);
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  // metadata: m, n, a_off (int64), v_off, t_off, order
+  std::vector<long long> aoff(count);
+  std::vector<int> meta(5 * (size_t)count);
+  int* hm = meta.data();
+  int* hn = hm + count;
+  int* hv = hn + count;
+  int* ht = hv + count;
+  int* ho = ht + count;
+  long long ao = 0;
+  int vo = 0, to = 0;
+  std::vector<std::pair<double, int>> work(count);
+  for (int i = 0; i < count; ++i) {
+    hm[i] = m[i];
+    hn[i] = n[i];
+    aoff[i] = ao;
+    hv[i] = vo;
+    ht[i] = to;
+    ao += (long long)m[i] * n[i];
+    vo += n[i];
+    to += std::min(m[i], n[i]);
+    const double mm = std::max(m[i], n[i]), nn = std::min(m[i], n[i]);
+    work[i] = {-(2.0 * mm * nn * nn - 2.0 * nn * nn * nn / 3.0), i};
+  }
+  std::stable_sort(work.begin(), work.end());
+  for (int i = 0; i < count; ++i) ho[i] = work[i].second;
+  const size_t meta_bytes = sizeof(long long) * count + sizeof(int) * meta.size() + sizeof(int) * 4;
+  const int grid = c->nsm;
+  const long long wsd = batched_ws_doubles(nmax);
+  unsigned long long key = 1469598103934665603ull;
+  key = fnv1a(key, meta.data(), sizeof(int) * meta.size());
+  void* ptrs[5] = {d_a, d_jpvt, d_tau, d_ncols, d_info};
+  key = fnv1a(key, ptrs, sizeof ptrs);
+  key = fnv1a(key, thres, sizeof(double) * 3);
+  key = fnv1a(key, &nb, sizeof nb);
+  key = fnv1a(key, &stop, sizeof stop);
+  if (c->b_graph && key == c->b_key && c->b_meta.cap >= meta_bytes &&
+      c->b_ws.cap >= sizeof(double) * (size_t)grid * wsd) {
+    // identical batch description: replay the captured launch
+    CK(cudaGraphLaunch(c->b_graph, s));
+    CK(cudaStreamSynchronize(s));
+    return 0;
+  }
+  CK(c->b_meta.ensure(meta_bytes));
+  CK(c->b_ws.ensure(sizeof(double) * (size_t)grid * wsd));
+  long long* d_aoff = c->b_meta.as<long long>();
+  int* d_meta = reinterpret_cast<int*>(d_aoff + count);
+  int* d_queue = d_meta + meta.size();
+  CK(cudaMemcpyAsync(d_aoff, aoff.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
+  BatchLaunch L;
+  L.m = d_meta;
+  L.n = d_meta + count;
+  L.a_off = d_aoff;
+  L.v_off = d_meta + 2 * count;
+  L.t_off = d_meta + 3 * count;
+  L.order = d_meta + 4 * count;
+  L.count = count;
+  L.A = d_a;
+  L.jpvt = d_jpvt;
+  L.tau = d_tau;
+  L.ncols = d_ncols;
+  L.info = d_info;
+  L.delta = delta;
+  L.tau_rel = tau_;
+  L.eta3 = thres[2];
+  L.nb = nb;
+  L.stop = stop;
+  L.ws = c->b_ws.as<double>();
+  L.ws_stride = wsd;
+  L.queue = d_queue;
+  L.grid = grid;
+  // capture the reset + launch once; later identical calls replay it
+  if (c->b_graph) {
+    cudaGraphExecDestroy(c->b_graph);
+    c->b_graph = nullptr;
+    c->b_key = 0;
+  }
+  cudaGraph_t graph = nullptr;
+  bool captured = false;
+  // recorded on the library's own stream (never the legacy default stream,
+  // which cannot be captured), replayed on the caller's stream
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  const bool can_capture = c->own != nullptr && cudaStreamIsCapturing(s, &cs) == cudaSuccess &&
+                           cs == cudaStreamCaptureStatusNone;
+  if (can_capture && cudaStreamBeginCapture(c->own, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const int lr = launch_batched(L, c->own);
+    if (cudaStreamEndCapture(c->own, &graph) == cudaSuccess && lr == 0 && graph) {
+      if (cudaGraphInstantiate(&c->b_graph, graph, 0) == cudaSuccess) {
+        captured = true;
+        c->b_key = key;
+      }
+    }
+    if (graph) cudaGraphDestroy(graph);
+    cudaGetLastError();
+  }
+  if (captured) {
+    CK(cudaGraphLaunch(c->b_graph, s));
+  } else if (launch_batched(L, s)) {
+    return QRDM_ERR_CUDA;
+  }
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
 int qrdm_set_stream(void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx* c = nullptr;
@@ -1020,7 +1153,12 @@ int qrdm_release_workspace(void) {
   Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
                  &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
                  &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst,
-                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp};
+                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws};
+  if (c.b_graph) {
+    cudaGraphExecDestroy(c.b_graph);
+    c.b_graph = nullptr;
+    c.b_key = 0;
+  }
   for (Buf* b : bufs) b->release();
   return 0;
 }

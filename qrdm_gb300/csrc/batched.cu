@@ -1,0 +1,648 @@
+// batched.cu -- many independent DM-QR problems of uneven size in one
+// persistent kernel.
+//
+// Each CTA takes the next problem from a device-side queue (problems ordered
+// by decreasing flop count, so the largest start first) and runs the whole
+// reference algorithm of dgeqrdm_work (src/dgeqrdm_work.c:672-787) on it with
+// CTA-level synchronisation only: norm initialisation, the DM candidate sort
+// and cosine Gram, the greedy pick and the permute_marked exchange sequence,
+// the dgeqr2_mia panel with its early exit, the T factor, the dlarfb
+// trailing update, the partial-norm downdate with its recompute safeguard and
+// the stop test.  Problem state (partial norms, the block record, W) lives in
+// per-CTA device workspace and shared memory; the matrices stay in global
+// memory (L2-resident while a CTA works on them).  Arithmetic is FP64: on
+// GB300 every phase is bound by the FP64 pipe, which one CTA of 256 threads
+// keeps busy with 4x4 register tiles.
+#include "common.cuh"
+#include "kernels.cuh"
+
+namespace qrdm {
+
+constexpr int BT = 256;            // threads per CTA
+constexpr int BNMAX = 1024;        // largest n of a batched problem
+constexpr int BKMAX = 64;          // largest DM block of a batched problem
+
+struct BatchShared {
+  Cand cand[BNMAX];
+  double g[64 * 65];        // cosine Gram / V^T V
+  double T[64 * 64];
+  double stage[2][32 * 65]; // row tiles of two operands
+  double red[BT];
+  double tw[BKMAX];
+  double sc[BKMAX];
+  double jv_n[4 * BKMAX + 8];
+  int jv_j[4 * BKMAX + 8];
+  int2 perm[4 * BKMAX + 8];
+  int sel[BKMAX], pos[BKMAX], swa[2 * BKMAX + 2], swb[2 * BKMAX + 2];
+  unsigned bits[BNMAX / 32];
+  int list[BNMAX];
+  double maxv, eta, alpha, tau, scal, beta, thres;
+  int nc, nsel, nswap, np, nlist, flag, exit_flag, tau_zero, next, stop_mode, nan;
+};
+
+__device__ __forceinline__ double block_sum(double v, double* red) {
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  double t = 0.0;
+  for (int q = 0; q < (int)(blockDim.x >> 5); ++q) t += red[q];
+  return t;
+}
+
+__device__ __forceinline__ bool cand_less(const Cand& a, const Cand& b) {
+  return a.val > b.val || (a.val == b.val && a.idx < b.idx);
+}
+
+__device__ void cta_bitonic(Cand* s, int N) {
+  for (int k = 2; k <= N; k <<= 1) {
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int t = threadIdx.x; t < N / 2; t += blockDim.x) {
+        int lo = 2 * jj * (t / jj) + (t % jj);
+        int hi = lo + jj;
+        bool up = ((lo & k) == 0);
+        Cand a = s[lo], b = s[hi];
+        if (up ? cand_less(b, a) : cand_less(a, b)) {
+          s[lo] = b;
+          s[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+__device__ __forceinline__ double pow2_for(double nrm) {
+  if (!(nrm > 0.0) || !(nrm < 1.7976931348623157e308)) return 1.0;
+  int e;
+  frexp(nrm, &e);
+  return ldexp(1.0, -e);
+}
+
+// G[p][q] = sum_{r in [0, len)} f(r, p) f(r, q), p, q < 64, via 32-row
+// shared-memory stages and 4x4 register tiles (256 threads).  Result in g
+// (row stride 65).
+template <class F>
+__device__ void cta_gram64(int len, F f, double* stage, double* g) {
+  const int tp = threadIdx.x / 16, tq = threadIdx.x % 16;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
+  for (int r0 = 0; r0 < len; r0 += 32) {
+    for (int e = threadIdx.x; e < 32 * 64; e += blockDim.x) {
+      const int p = e / 32, rr = e % 32;
+      const int r = r0 + rr;
+      stage[rr * 65 + p] = r < len ? f(r, p) : 0.0;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int rr = 0; rr < 32; ++rr) {
+      double x[4], y[4];
+#pragma unroll
+      for (int a = 0; a < 4; ++a) x[a] = stage[rr * 65 + tp + 16 * a];
+#pragma unroll
+      for (int b = 0; b < 4; ++b) y[b] = stage[rr * 65 + tq + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+#pragma unroll
+        for (int b = 0; b < 4; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b) g[(tp + 16 * a) * 65 + tq + 16 * b] = acc[a][b];
+  __syncthreads();
+}
+
+struct BatchArgs {
+  const int* m;
+  const int* n;
+  const long long* a_off;  // column-major, lda = m
+  const int* v_off;        // jpvt / ncols offsets (n ints each)
+  const int* t_off;        // tau offsets (min(m, n) each)
+  const int* order;        // problems in processing order
+  int count;
+  double* A;
+  int* jpvt;
+  double* tau;
+  int* ncols;
+  int* info;
+  double delta, tau_rel, eta3;
+  int nb, stop;
+  double* ws;          // per-CTA workspace: nrm, nrm_exact, W (64 x nmax)
+  long long ws_stride;
+  int* queue;
+};
+
+__device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws) {
+  const int m = a.m[p], n = a.n[p];
+  double* A = a.A + a.a_off[p];
+  const long long lda = m;
+  int* jp = a.jpvt + a.v_off[p];
+  int* ncols = a.ncols + a.v_off[p];
+  double* tau = a.tau + a.t_off[p];
+  double* nrm = ws;
+  double* nrmx = ws + BNMAX;
+  double* W = ws + 2 * BNMAX;  // [64][n]
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5, nw = blockDim.x >> 5;
+  const int minmn = min(m, n);
+  if (tid == 0) {
+    S.stop_mode = a.stop;
+    S.nan = 0;
+    S.maxv = 0.0;
+  }
+  for (int c = tid; c < n; c += blockDim.x) {
+    jp[c] = c + 1;
+    ncols[c] = 0;
+  }
+  __syncthreads();
+  // ---- norm init
+  for (int c = wid; c < n; c += nw) {
+    const double v = column_norm_warp(A + (size_t)c * lda, m, lane);
+    if (lane == 0) {
+      nrm[c] = v;
+      nrmx[c] = v;
+      if (v != v) atomicExch(&S.nan, 1);
+    }
+  }
+  __syncthreads();
+  double mx = 0.0;
+  for (int c = tid; c < n; c += blockDim.x) mx = fmax(mx, nrm[c]);
+  mx = warp_max(mx);
+  if (lane == 0) S.red[wid] = mx;
+  __syncthreads();
+  if (tid == 0) {
+    double t = 0.0;
+    for (int q = 0; q < nw; ++q) t = fmax(t, S.red[q]);
+    const double eps = QRDM_EPS64;
+    double eta = 0.0;
+    if (S.stop_mode == 1) eta = eps * n;
+    else if (S.stop_mode == 2) eta = eps * sqrt((double)n);
+    else if (S.stop_mode == 3) eta = a.eta3;
+    S.eta = eta * t;
+  }
+  __syncthreads();
+  if (S.nan) {
+    if (tid == 0 && a.info) a.info[p] = -13;
+    return;
+  }
+  int j = 0, it = 0;
+  while (j < minmn) {
+    const int mloc = m - j, nloc = n - j;
+    const int kmax = min(min(a.nb, mloc), nloc);
+    double* W0 = A + (size_t)j * lda + j;
+    // ---- candidates: sort (norm desc, index asc), nc
+    int P = 32;
+    while (P < nloc) P <<= 1;
+    for (int t = tid; t < P; t += blockDim.x) {
+      Cand c;
+      if (t < nloc) {
+        c.val = nrm[j + t];
+        c.idx = t;
+      } else {
+        c.val = -1.0;
+        c.idx = 0x7fffffff;
+      }
+      c.pad = 0;
+      S.cand[t] = c;
+    }
+    __syncthreads();
+    cta_bitonic(S.cand, P);
+    if (tid == 0) {
+      const double cut = a.tau_rel * S.cand[0].val;
+      int nc = 0;
+      while (nc < nloc && nc < kmax && S.cand[nc].val > cut) ++nc;
+      S.nc = nc;
+    }
+    __syncthreads();
+    const int nc = S.nc;
+    // ---- cosine Gram of the scaled candidates
+    if (nc > 1) {
+      if (tid < 64) S.tw[tid] = tid < nc ? 1.0 / S.cand[tid].val : 0.0;
+      __syncthreads();
+      auto f = [&](int r, int q) -> double {
+        return q < nc ? S.tw[q] * W0[(size_t)S.cand[q].idx * lda + r] : 0.0;
+      };
+      cta_gram64(mloc, f, S.stage[0], S.g);
+    }
+    // ---- greedy pick (warp 0) and permute_marked replay (thread 0)
+    const int nwords = (nloc + 31) >> 5;
+    for (int w = tid; w < nwords; w += blockDim.x) S.bits[w] = 0u;
+    __syncthreads();
+    if (wid == 0) {
+      int nsel = 1;
+      if (lane == 0) {
+        S.sel[0] = S.cand[0].idx;
+        S.pos[0] = 0;
+      }
+      __syncwarp();
+      for (int i = 1; i < nc; ++i) {
+        double worst = 0.0;
+        for (int q = lane; q < nsel; q += 32) worst = fmax(worst, fabs(S.g[S.pos[q] * 65 + i]));
+        worst = warp_max(worst);
+        if (worst < a.delta && nsel < kmax) {
+          if (lane == 0) {
+            S.pos[nsel] = i;
+            S.sel[nsel] = S.cand[i].idx;
+          }
+          ++nsel;
+        }
+        __syncwarp();
+      }
+      if (lane == 0) S.nsel = nsel;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      const int nsel = S.nsel;
+      unsigned* bits = S.bits;
+      for (int q = 0; q < nsel; ++q) bits[S.sel[q] >> 5] |= 1u << (S.sel[q] & 31);
+#define BMARK(x) ((bits[(x) >> 5] >> ((x) & 31)) & 1u)
+      const int maxsw = 2 * BKMAX + 2;
+      int nswap = 0, jb = 0, jt = nloc - 1;
+      auto xchg = [&](int x, int y) {
+        if (BMARK(x) != BMARK(y)) {
+          bits[x >> 5] ^= 1u << (x & 31);
+          bits[y >> 5] ^= 1u << (y & 31);
+        }
+        if (nswap < maxsw) {
+          S.swa[nswap] = x;
+          S.swb[nswap] = y;
+        }
+        ++nswap;
+      };
+      for (int q = 0; q < nsel; ++q) {
+        const int jc = S.sel[q];
+        while (jb < jt && BMARK(jt) == 1u) {
+          xchg(jt, jb);
+          while (jb < nloc && BMARK(jb) == 1u) ++jb;
+        }
+        if (BMARK(jc) != 1u) continue;
+        while (jb < nloc && BMARK(jb) == 1u) ++jb;
+        if (jc <= jb || jc < nsel) continue;
+        if (BMARK(jb) == 0u) {
+          xchg(jc, jb);
+          ++jb;
+        }
+      }
+#undef BMARK
+      if (nswap > maxsw) nswap = 0;  // cannot happen: at most 2 nsel + 1 exchanges
+      S.nswap = nswap;
+      // composed permutation: first occurrence of each exchanged position
+      int np = 0;
+      for (int e = 0; e < 2 * nswap; ++e) {
+        const int s = e >> 1;
+        const int dst = (e & 1) ? S.swb[s] : S.swa[s];
+        bool keep = true;
+        for (int t = 0; t < s && keep; ++t)
+          if (S.swa[t] == dst || S.swb[t] == dst) keep = false;
+        if (keep && (e & 1) && S.swa[s] == dst) keep = false;
+        if (!keep) continue;
+        int x = dst;
+        for (int t = nswap - 1; t >= 0; --t) {
+          if (x == S.swa[t]) x = S.swb[t];
+          else if (x == S.swb[t]) x = S.swa[t];
+        }
+        if (x != dst) S.perm[np++] = make_int2(dst, x);
+      }
+      S.np = np;
+    }
+    __syncthreads();
+    const int np = S.np, fjb = S.nsel;
+    // jpvt and partial norms (not the exact norms, like the reference)
+    for (int e = tid; e < np; e += blockDim.x) {
+      S.jv_j[e] = jp[j + S.perm[e].y];
+      S.jv_n[e] = nrm[j + S.perm[e].y];
+    }
+    __syncthreads();
+    for (int e = tid; e < np; e += blockDim.x) {
+      jp[j + S.perm[e].x] = S.jv_j[e];
+      nrm[j + S.perm[e].x] = S.jv_n[e];
+    }
+    // whole columns (all m rows), staged `rc` rows at a time through the
+    // 2 x 32 x 65-double stage area
+    const int rc = np > 0 ? max(1, min(32, (2 * 32 * 65) / np)) : 1;
+    for (int r0 = 0; r0 < m && np > 0; r0 += rc) {
+      double* st = S.stage[0];
+      for (int e = tid; e < np * rc; e += blockDim.x) {
+        const int t = e / rc, rr = e % rc, r = r0 + rr;
+        if (r < m) st[t * rc + rr] = A[(size_t)(j + S.perm[t].y) * lda + r];
+      }
+      __syncthreads();
+      for (int e = tid; e < np * rc; e += blockDim.x) {
+        const int t = e / rc, rr = e % rc, r = r0 + rr;
+        if (r < m) A[(size_t)(j + S.perm[t].x) * lda + r] = st[t * rc + rr];
+      }
+      __syncthreads();
+    }
+    __syncthreads();
+    // ---- panel (dgeqr2_mia) with early exit, columns scaled by 2^-e
+    for (int c = tid; c < fjb; c += blockDim.x) S.sc[c] = pow2_for(nrm[j + c]);
+    if (tid == 0) {
+      S.thres = 5e-14;
+      S.exit_flag = 0;
+    }
+    __syncthreads();
+    int kc = fjb;
+    for (int i = 0; i < fjb; ++i) {
+      const double sci = S.sc[i];
+      const double* x = W0 + (size_t)i * lda;
+      const int nslot = fjb - i;
+      for (int sl = wid; sl < nslot; sl += nw) {
+        const double* y = W0 + (size_t)(i + sl) * lda;
+        double acc = 0.0;
+        for (int r = i + 1 + lane; r < mloc; r += 32) {
+          const double xs = x[r] * sci;
+          acc = fma(xs, sl == 0 ? xs : y[r], acc);
+        }
+        acc = warp_sum(acc);
+        if (lane == 0) S.red[sl] = acc;
+      }
+      __syncthreads();
+      if (tid == 0) {
+        const double alpha = x[i] * sci;
+        S.tau_zero = 1;
+        S.tau = 0.0;
+        S.scal = 0.0;
+        S.beta = x[i];
+        if (mloc - i > 1) {
+          const double xs = sqrt(S.red[0]);
+          if (i > 0 && xs / sci < S.thres) {
+            S.exit_flag = 1;
+          } else if (xs != 0.0) {
+            const double bs = -sign_of(hypot_lapack(alpha, xs), alpha);
+            S.tau = (bs - alpha) / bs;
+            S.scal = 1.0 / (alpha - bs);
+            S.beta = bs / sci;
+            S.tau_zero = 0;
+          }
+        }
+        if (!S.exit_flag) {
+          if (i == 0 && fjb > 1 && a.tau_rel > 0.0) S.thres = a.tau_rel * fabs(S.beta);
+          tau[j + i] = S.tau;
+        }
+      }
+      __syncthreads();
+      if (S.exit_flag) {
+        kc = i;
+        break;
+      }
+      if (!S.tau_zero) {
+        // w_c = C_c(i) + scal (x sc . C_c): C columns unscaled
+        for (int c = i + 1 + tid; c < fjb; c += blockDim.x) {
+          const double w = W0[(size_t)c * lda + i] + S.scal * S.red[c - i];
+          S.tw[c] = S.tau * w;
+        }
+        __syncthreads();
+        const double vs = sci * S.scal;
+        double* xw = W0 + (size_t)i * lda;
+        for (int r = i + tid; r < mloc; r += blockDim.x) {
+          if (r == i) {
+            for (int c = i + 1; c < fjb; ++c) W0[(size_t)c * lda + r] -= S.tw[c];
+          } else {
+            const double v = xw[r] * vs;
+            xw[r] = v;
+            for (int c = i + 1; c < fjb; ++c) W0[(size_t)c * lda + r] = fma(-v, S.tw[c], W0[(size_t)c * lda + r]);
+          }
+        }
+        __syncthreads();
+        if (tid == 0) xw[i] = S.beta;
+      }
+      __syncthreads();
+    }
+    // ---- T factor: V^T V then the forward recurrence
+    if (kc > 1) {
+      auto fv = [&](int r, int q) -> double {
+        return q < kc ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
+      };
+      cta_gram64(mloc, fv, S.stage[0], S.g);
+    }
+    for (int e = tid; e < 64 * 64; e += blockDim.x) S.T[e] = 0.0;
+    __syncthreads();
+    {
+      const int ar = tid >> 2, part = tid & 3;
+      for (int i = 0; i < kc; ++i) {
+        const double ti = tau[j + i];
+        if (tid < i) S.red[tid] = -ti * S.g[tid * 65 + i];
+        __syncthreads();
+        double acc = 0.0;
+        if (ar < i && ti != 0.0)
+          for (int b = ar + part; b < i; b += 4) acc = fma(S.T[b * 64 + ar], S.red[b], acc);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+        acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+        if (ar < i && part == 0) S.T[i * 64 + ar] = acc;
+        if (tid == 0) S.T[i * 64 + i] = ti;
+        __syncthreads();
+      }
+    }
+    // ---- trailing update C <- (I - V T V^T)^T C, C = window columns fjb..
+    const int n2 = nloc - fjb;
+    if (kc > 0 && n2 > 0) {
+      const int ta = tid / 16, tc = tid % 16;
+      for (int c0 = 0; c0 < n2; c0 += 64) {
+        // W = V^T C(:, c0..c0+63)
+        double acc[4][4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) acc[x][y] = 0.0;
+        for (int r0 = 0; r0 < mloc; r0 += 32) {
+          for (int e = tid; e < 32 * 64; e += blockDim.x) {
+            const int q = e / 32, rr = e % 32, r = r0 + rr;
+            const double v = (q < kc && r < mloc) ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
+            S.stage[0][rr * 65 + q] = v;
+            const int c = c0 + q;
+            S.stage[1][rr * 65 + q] = (c < n2 && r < mloc) ? W0[(size_t)(fjb + c) * lda + r] : 0.0;
+          }
+          __syncthreads();
+#pragma unroll 4
+          for (int rr = 0; rr < 32; ++rr) {
+            double v[4], cv[4];
+#pragma unroll
+            for (int x = 0; x < 4; ++x) v[x] = S.stage[0][rr * 65 + ta + 16 * x];
+#pragma unroll
+            for (int y = 0; y < 4; ++y) cv[y] = S.stage[1][rr * 65 + tc + 16 * y];
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+              for (int y = 0; y < 4; ++y) acc[x][y] = fma(v[x], cv[y], acc[x][y]);
+          }
+          __syncthreads();
+        }
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) S.g[(ta + 16 * x) * 65 + tc + 16 * y] = acc[x][y];
+        __syncthreads();
+        // W2 = T^T W  -> stage[1] as [a][c]
+        for (int e = tid; e < 64 * 64; e += blockDim.x) {
+          const int aa = e / 64, cc = e % 64;
+          double s2 = 0.0;
+          if (aa < kc)
+            for (int b = 0; b <= aa; ++b) s2 = fma(S.T[aa * 64 + b], S.g[b * 65 + cc], s2);
+          if (c0 + cc < n2) W[(size_t)aa * n + c0 + cc] = s2;
+        }
+        __syncthreads();
+        // C -= V W2, 64-row tiles (rows fastest across threads)
+        const int tr = tid % 16, tcc = tid / 16;
+        for (int r0 = 0; r0 < mloc; r0 += 64) {
+          double u[4][4];
+#pragma unroll
+          for (int x = 0; x < 4; ++x)
+#pragma unroll
+            for (int y = 0; y < 4; ++y) u[x][y] = 0.0;
+          for (int q0 = 0; q0 < kc; q0 += 32) {
+            for (int e = tid; e < 32 * 64; e += blockDim.x) {
+              const int qq = e / 64, rr = e % 64, q = q0 + qq, r = r0 + rr;
+              S.stage[0][qq * 65 + rr] =
+                  (q < kc && r < mloc) ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
+              const int cc = rr;
+              S.stage[1][qq * 65 + cc] = (q < kc && c0 + cc < n2) ? W[(size_t)q * n + c0 + cc] : 0.0;
+            }
+            __syncthreads();
+#pragma unroll 8
+            for (int qq = 0; qq < 32; ++qq) {
+              double v[4], w[4];
+#pragma unroll
+              for (int x = 0; x < 4; ++x) v[x] = S.stage[0][qq * 65 + tr + 16 * x];
+#pragma unroll
+              for (int y = 0; y < 4; ++y) w[y] = S.stage[1][qq * 65 + tcc + 16 * y];
+#pragma unroll
+              for (int x = 0; x < 4; ++x)
+#pragma unroll
+                for (int y = 0; y < 4; ++y) u[x][y] = fma(v[x], w[y], u[x][y]);
+            }
+            __syncthreads();
+          }
+#pragma unroll
+          for (int y = 0; y < 4; ++y) {
+            const int c = c0 + tcc + 16 * y;
+            if (c >= n2) continue;
+#pragma unroll
+            for (int x = 0; x < 4; ++x) {
+              const int r = r0 + tr + 16 * x;
+              if (r < mloc) W0[(size_t)(fjb + c) * lda + r] -= u[x][y];
+            }
+          }
+        }
+        __syncthreads();
+      }
+    }
+    // ---- partial-norm downdate (norm_update) and recomputes
+    if (tid == 0) {
+      S.nlist = 0;
+      S.maxv = 0.0;
+    }
+    __syncthreads();
+    const double tol3z = 1.0536712127723509e-08;
+    double lmax = 0.0;
+    for (int c = j + kc + tid; c < n; c += blockDim.x) {
+      double w = nrm[c];
+      if (w == 0.0) continue;
+      const double* col = A + (size_t)c * lda + j;
+      double s2 = 0.0;
+      for (int i = 0; i < kc; ++i) s2 = mul_add_rn(col[i], col[i], s2);
+      double t = sqrt(fabs(s2)) / w;
+      double d2 = (t + 1.0) * (1.0 - t);
+      t = (0.0 >= d2) ? 0.0 : d2;
+      double rr = w / nrmx[c];
+      double t2 = t * (rr * rr);
+      if (t2 <= tol3z) {
+        const int slot = atomicAdd(&S.nlist, 1);
+        S.list[slot] = c;
+      } else {
+        w *= sqrt(t);
+        nrm[c] = w;
+        lmax = fmax(lmax, w);
+      }
+    }
+    __syncthreads();
+    const int r0n = j + kc;
+    for (int q = wid; q < S.nlist; q += nw) {
+      const int c = S.list[q];
+      const double v = (m - r0n) > 0 ? column_norm_warp(A + (size_t)c * lda + r0n, m - r0n, lane) : 0.0;
+      if (lane == 0) {
+        nrm[c] = v;
+        nrmx[c] = v;
+      }
+      lmax = lane == 0 ? fmax(lmax, v) : lmax;
+    }
+    lmax = warp_max(lmax);
+    __syncthreads();
+    if (lane == 0) S.red[wid] = lmax;
+    __syncthreads();
+    if (tid == 0) {
+      double t = 0.0;
+      for (int q = 0; q < nw; ++q) t = fmax(t, S.red[q]);
+      S.maxv = t;
+      ncols[it] = kc;
+    }
+    __syncthreads();
+    ++it;
+    j += kc;
+    if (S.stop_mode >= 1 && S.stop_mode <= 3) {
+      if (S.maxv * sqrt((double)(nloc - kc)) <= S.eta) break;
+    }
+    if (kc <= 0) break;  // cannot happen: the first panel column never exits
+  }
+  if (tid == 0 && a.info) a.info[p] = 0;
+}
+
+__global__ void __launch_bounds__(BT, 1) k_dmqr_batched(BatchArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  BatchShared& S = *reinterpret_cast<BatchShared*>(smem_raw);
+  double* ws = a.ws + (size_t)blockIdx.x * a.ws_stride;
+  while (true) {
+    if (threadIdx.x == 0) S.next = atomicAdd(a.queue, 1);
+    __syncthreads();
+    const int q = S.next;
+    __syncthreads();
+    if (q >= a.count) break;
+    solve_one(a, a.order[q], S, ws);
+    __syncthreads();
+  }
+}
+
+size_t batched_smem_bytes() { return sizeof(BatchShared); }
+int batched_nmax() { return BNMAX; }
+int batched_kmax() { return BKMAX; }
+long long batched_ws_doubles(int nmax) { return 2LL * BNMAX + 64LL * nmax; }
+
+int batched_set_attributes() {
+  return cudaFuncSetAttribute(k_dmqr_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(BatchShared)) == cudaSuccess ? 0 : 1;
+}
+
+// Enqueue the persistent batched kernel (queue counter reset + launch).
+int launch_batched(const BatchLaunch& L, cudaStream_t s) {
+  BatchArgs a;
+  a.m = L.m;
+  a.n = L.n;
+  a.a_off = L.a_off;
+  a.v_off = L.v_off;
+  a.t_off = L.t_off;
+  a.order = L.order;
+  a.count = L.count;
+  a.A = L.A;
+  a.jpvt = L.jpvt;
+  a.tau = L.tau;
+  a.ncols = L.ncols;
+  a.info = L.info;
+  a.delta = L.delta;
+  a.tau_rel = L.tau_rel;
+  a.eta3 = L.eta3;
+  a.nb = L.nb;
+  a.stop = L.stop;
+  a.ws = L.ws;
+  a.ws_stride = L.ws_stride;
+  a.queue = L.queue;
+  if (cudaMemsetAsync(L.queue, 0, sizeof(int), s) != cudaSuccess) return 1;
+  k_dmqr_batched<<<L.grid, BT, sizeof(BatchShared), s>>>(a);
+  return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+}  // namespace qrdm

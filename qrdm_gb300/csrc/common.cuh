@@ -115,3 +115,48 @@ __device__ __forceinline__ double sign_of(double mag, double s) {
 #define QRDM_SFMIN64 2.2250738585072014e-308
 
 __host__ __device__ __forceinline__ int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+// ||col[0:len)|| by one warp: FP64 sum of squares over 16-byte loads and
+// shuffles; columns whose sum of squares leaves [2^-960, 2^960] are redone
+// with a power-of-two scale (overflow/underflow-safe, like dnrm2).
+__device__ __forceinline__ double column_sumsq(const double* __restrict__ col, int len, int lane) {
+  double s = 0.0;
+  // peel to a 16-byte boundary
+  int head = (int)(((16 - ((uintptr_t)col & 15)) & 15) >> 3);
+  if (head > len) head = len;
+  if (lane < head) s = col[lane] * col[lane];
+  const double2* v = reinterpret_cast<const double2*>(col + head);
+  int nv = (len - head) >> 1;
+  for (int k = lane; k < nv; k += 32) {
+    double2 x = __ldg(v + k);
+    s = fma(x.x, x.x, s);
+    s = fma(x.y, x.y, s);
+  }
+  int tail = head + 2 * nv;
+  if (tail + lane < len) s = fma(col[tail + lane], col[tail + lane], s);
+  return warp_sum(s);
+}
+
+__device__ __forceinline__ double column_norm_warp(const double* __restrict__ col, int len, int lane) {
+  double s = column_sumsq(col, len, lane);
+  if (s != s) return s;                          // NaN propagates
+  if (s >= 0x1p-960 && s <= 0x1p960) return sqrt(s);
+  if (s == 0.0) return 0.0;
+  // scaled path: mx = max |x|; norm = mx * sqrt(sum (x/mx)^2)
+  double mx = 0.0;
+  for (int k = lane; k < len; k += 32) mx = fmax(mx, fabs(col[k]));
+  mx = warp_max(mx);
+  if (mx == 0.0 || mx > 1.7976931348623157e308) return mx;
+  int e;
+  frexp(mx, &e);
+  double sc = ldexp(1.0, -e);
+  double t = 0.0;
+  for (int k = lane; k < len; k += 32) {
+    double y = col[k] * sc;
+    t = fma(y, y, t);
+  }
+  t = warp_sum(t);
+  return sqrt(t) * ldexp(1.0, e);
+}
+
+

@@ -102,6 +102,31 @@ int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, in
 void oz_workspace(int m, int n, int s, int nsm, size_t* va2, size_t* vb1, size_t* wb2, size_t* wexp,
                   size_t* wp);
 
+// batched.cu
+struct BatchLaunch {
+  const int *m, *n;
+  const long long* a_off;
+  const int *v_off, *t_off, *order;
+  int count;
+  double* A;
+  int* jpvt;
+  double* tau;
+  int* ncols;
+  int* info;
+  double delta, tau_rel, eta3;
+  int nb, stop;
+  double* ws;
+  long long ws_stride;
+  int* queue;
+  int grid;
+};
+int batched_set_attributes();
+int launch_batched(const BatchLaunch& L, cudaStream_t s);
+size_t batched_smem_bytes();
+int batched_nmax();
+int batched_kmax();
+long long batched_ws_doubles(int nmax);
+
 // qp3.cu
 struct Qp3State;
 size_t qp3_state_bytes();
