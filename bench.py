@@ -437,13 +437,13 @@ def batched_problem_device(i, m, n, seed=4):
     return a.T.contiguous().view(-1)
 
 
-def batched_setup(seed=4):
+def batched_setup(seed=4, count=None):
     import torch
 
     from qrdm_gb300 import BatchedDMQR
     from qrdm_gb300.workloads import batched_shapes
 
-    ms, ns = batched_shapes(BATCH_COUNT, seed=seed)
+    ms, ns = batched_shapes(count or BATCH_COUNT, seed=seed)
     shapes = [(int(m), int(n)) for m, n in zip(ms, ns)]
     b = BatchedDMQR(shapes)
     for i, (m, n) in enumerate(shapes):
@@ -511,7 +511,8 @@ def run_batched(args):
     L = lib()
     stream = torch.cuda.current_stream()
     L.qrdm_set_stream(C.c_void_p(stream.cuda_stream))
-    b, shapes = batched_setup()
+    b, shapes = batched_setup(count=args.count)
+    count = len(shapes)
     pristine = b.a.clone()
     launches_per_step = 1
 
@@ -537,7 +538,7 @@ def run_batched(args):
         torch.cuda.synchronize()
         barrier(world)
     ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world)
-    value = world * BATCH_COUNT / (ms / 1e3)
+    value = world * count / (ms / 1e3)
     clocks = clk.summary()
     if rank == 0:
         peaks, peak_kind = load_peaks()
@@ -552,6 +553,13 @@ def run_batched(args):
         e1.record(stream)
         torch.cuda.synchronize()
         kms = e0.elapsed_time(e1)
+        cyc = (C.c_ulonglong * 9)()
+        L.qrdm_batched_phase_cycles(cyc, 9)
+        names = ["norms", "select", "panel", "tfactor", "trail", "downdate", "queue"]
+        busy = float(cyc[7]) or 1.0
+        phases = {nm: float(cyc[k]) / busy for k, nm in enumerate(names)}
+        nsm = torch.cuda.get_device_properties(local).multi_processor_count
+        phases["longest_over_mean_cta"] = float(cyc[8]) / (busy / nsm)
         be, orth = batched_errors(b, pristine)
         achieved = F / (kms / 1e3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch)",
@@ -559,7 +567,7 @@ def run_batched(args):
                 "peak_kind": "nominal FP64 (no measured FP64 peak); HBM term from measured "
                              f"{peaks['hbm_gbs']} GB/s", "unit": "TFLOP/s",
                 "frac": t_roof / (kms / 1e3),
-                "summed_roofline_mats_per_s": BATCH_COUNT / t_roof,
+                "summed_roofline_mats_per_s": count / t_roof,
                 "traffic": load_traffic("dmqr_batched"),
                 "per_launch_basis": "sum_i 2 m_i n_i^2 - 2 n_i^3 / 3 flops over 2000 problems"}
         # e2e: pinned host buffer -> device, factor, factors back to the host
@@ -579,7 +587,7 @@ def run_batched(args):
             e2e_t.append(time.perf_counter() - t0)
         h2d = 8 * pristine.numel()
         d2h = 8 * pristine.numel() + 4 * b.jpvt.numel() + 8 * b.tau.numel()
-        e2e = {"value": world * BATCH_COUNT / min(e2e_t), "unit": "matrices/s",
+        e2e = {"value": world * count / min(e2e_t), "unit": "matrices/s",
                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
         cpu = None
         if args.cpu_baseline:
@@ -592,13 +600,14 @@ def run_batched(args):
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic",
-               "config": {"workload": "batched2000", "count": BATCH_COUNT, "nb": BATCH_NB,
+               "config": {"workload": "batched2000", "count": count, "nb": BATCH_NB,
                           "delta": DELTA, "tau_": TAU_, "flops": F,
                           "bytes": 8 * pristine.numel(),
                           "parallelism": f"replicas{world}",
                           "l2": "inputs (3.3 GB) larger than L2; no flush needed"},
                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
                "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
+               "phase_share": phases,
                "errors": {"backward_p50": float(np.percentile(be, 50)),
                           "backward_p99": float(np.percentile(be, 99)),
                           "backward_max": float(be.max()),
@@ -653,6 +662,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="lowrank16k")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--no-variants", dest="variants", action="store_false")
+    ap.add_argument("--count", type=int, default=None,
+                    help="batched2000: number of problems (default 2000)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     if args.workload == "batched2000":

@@ -125,6 +125,12 @@ int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda, i
 int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int* d_jpvt, double* d_tau,
                         int* d_ncols, int* d_info, const double* thres, int stop, int nb);
 
+/* Device cycles spent by the last dgeqrdm_batched_dev call, summed over its
+ * CTAs: out[0..7] = norms, selection, panel, T factor, trailing update,
+ * downdate, queue, CTA lifetime; out[8] (if nout > 8) = the longest CTA
+ * lifetime.  Instrumentation only (no counterpart in the reference). */
+int qrdm_batched_phase_cycles(unsigned long long* out, int nout);
+
 /* ------------------------------------------------------------------ QP3 */
 /* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot
  * per column by largest partial norm, first index on ties; jpvt[j] != 0

@@ -1064,7 +1064,8 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   key = fnv1a(key, thres, sizeof(double) * 3);
   key = fnv1a(key, &nb, sizeof nb);
   key = fnv1a(key, &stop, sizeof stop);
-  if (c->b_graph && key == c->b_key && c->b_meta.cap >= meta_bytes &&
+  const size_t prof_bytes = sizeof(unsigned long long) * (size_t)grid * batched_phases();
+  if (c->b_graph && key == c->b_key && c->b_meta.cap >= meta_bytes && c->b_prof.cap >= prof_bytes &&
       c->b_ws.cap >= sizeof(double) * (size_t)grid * wsd) {
     // identical batch description: replay the captured launch
     CK(cudaGraphLaunch(c->b_graph, s));
@@ -1073,6 +1074,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   }
   CK(c->b_meta.ensure(meta_bytes));
   CK(c->b_ws.ensure(sizeof(double) * (size_t)grid * wsd));
+  CK(c->b_prof.ensure(prof_bytes));
   long long* d_aoff = c->b_meta.as<long long>();
   int* d_meta = reinterpret_cast<int*>(d_aoff + count);
   int* d_queue = d_meta + meta.size();
@@ -1099,6 +1101,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   L.ws = c->b_ws.as<double>();
   L.ws_stride = wsd;
   L.queue = d_queue;
+  L.prof = c->b_prof.as<unsigned long long>();
   L.grid = grid;
   // capture the reset + launch once; later identical calls replay it
   if (c->b_graph) {
@@ -1133,6 +1136,30 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   return 0;
 }
 
+int qrdm_batched_phase_cycles(unsigned long long* out, int nout) {
+  if (!out || nout <= 0) return -1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  const int ph = batched_phases();
+  for (int k = 0; k < nout; ++k) out[k] = 0;
+  if (!c->b_prof.p) return 0;
+  const int grid = c->nsm;
+  std::vector<unsigned long long> h((size_t)grid * ph);
+  CK(cudaMemcpyAsync(h.data(), c->b_prof.p, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost,
+                     c->stream()));
+  CK(cudaStreamSynchronize(c->stream()));
+  for (int b = 0; b < grid; ++b)
+    for (int k = 0; k < ph && k < nout; ++k) out[k] += h[(size_t)b * ph + k];
+  if (nout > ph) {
+    unsigned long long mx = 0;  // slowest CTA (makespan in cycles)
+    for (int b = 0; b < grid; ++b) mx = std::max(mx, h[(size_t)b * ph + ph - 1]);
+    out[ph] = mx;
+  }
+  return 0;
+}
+
 int qrdm_set_stream(void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx* c = nullptr;
@@ -1153,7 +1180,7 @@ int qrdm_release_workspace(void) {
   Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
                  &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
                  &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst,
-                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws};
+                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws, &c.b_prof};
   if (c.b_graph) {
     cudaGraphExecDestroy(c.b_graph);
     c.b_graph = nullptr;

@@ -22,11 +22,15 @@ constexpr int BT = 256;            // threads per CTA
 constexpr int BNMAX = 1024;        // largest n of a batched problem
 constexpr int BKMAX = 64;          // largest DM block of a batched problem
 
+// stage area: V (32 x (KW+1)) + C (32 x (CW+1)) tiles of the trailing
+// update, CW = 4096 / KW, KW in {32, 64}; also the Gram and swap staging
+constexpr int kStage = 32 * 33 + 32 * 129 + 32;
+
 struct BatchShared {
   Cand cand[BNMAX];
   double g[64 * 65];        // cosine Gram / V^T V
   double T[64 * 64];
-  double stage[2][32 * 65]; // row tiles of two operands
+  double stage[kStage];     // row tiles of the GEMM operands
   double red[BT];
   double tw[BKMAX];
   double sc[BKMAX];
@@ -80,43 +84,162 @@ __device__ __forceinline__ double pow2_for(double nrm) {
   return ldexp(1.0, -e);
 }
 
-// G[p][q] = sum_{r in [0, len)} f(r, p) f(r, q), p, q < 64, via 32-row
-// shared-memory stages and 4x4 register tiles (256 threads).  Result in g
-// (row stride 65).
-template <class F>
-__device__ void cta_gram64(int len, F f, double* stage, double* g) {
+// G[p][q] = sum_{r in [0, len)} f(r, p) f(r, q), p, q < KW (32 or 64), via
+// (2048 / KW)-row shared-memory stages and (KW/16) x (KW/16) register tiles
+// (256 threads).  Result in g (row stride 65).
+template <int KW, class F>
+__device__ void cta_gram(int len, F f, double* stage, double* g) {
+  constexpr int RS = 2048 / KW;  // rows per stage
+  constexpr int TT = KW / 16;    // register tile edge
+  constexpr int LD = KW + 1;
   const int tp = threadIdx.x / 16, tq = threadIdx.x % 16;
-  double acc[4][4];
+  double acc[TT][TT];
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < TT; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) acc[a][b] = 0.0;
-  for (int r0 = 0; r0 < len; r0 += 32) {
-    for (int e = threadIdx.x; e < 32 * 64; e += blockDim.x) {
-      const int p = e / 32, rr = e % 32;
+    for (int b = 0; b < TT; ++b) acc[a][b] = 0.0;
+  for (int r0 = 0; r0 < len; r0 += RS) {
+    for (int e = threadIdx.x; e < RS * KW; e += blockDim.x) {
+      const int p = e / RS, rr = e % RS;
       const int r = r0 + rr;
-      stage[rr * 65 + p] = r < len ? f(r, p) : 0.0;
+      stage[rr * LD + p] = r < len ? f(r, p) : 0.0;
     }
     __syncthreads();
 #pragma unroll 4
-    for (int rr = 0; rr < 32; ++rr) {
-      double x[4], y[4];
+    for (int rr = 0; rr < RS; ++rr) {
+      double x[TT], y[TT];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) x[a] = stage[rr * 65 + tp + 16 * a];
+      for (int a = 0; a < TT; ++a) x[a] = stage[rr * LD + tp + 16 * a];
 #pragma unroll
-      for (int b = 0; b < 4; ++b) y[b] = stage[rr * 65 + tq + 16 * b];
+      for (int b = 0; b < TT; ++b) y[b] = stage[rr * LD + tq + 16 * b];
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+      for (int a = 0; a < TT; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
+        for (int b = 0; b < TT; ++b) acc[a][b] = fma(x[a], y[b], acc[a][b]);
     }
     __syncthreads();
   }
 #pragma unroll
-  for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < TT; ++a)
 #pragma unroll
-    for (int b = 0; b < 4; ++b) g[(tp + 16 * a) * 65 + tq + 16 * b] = acc[a][b];
+    for (int b = 0; b < TT; ++b) g[(tp + 16 * a) * 65 + tq + 16 * b] = acc[a][b];
   __syncthreads();
+}
+
+template <class F>
+__device__ void cta_gram_any(int k, int len, F f, double* stage, double* g) {
+  if (k <= 32) cta_gram<32>(len, f, stage, g);
+  else cta_gram<64>(len, f, stage, g);
+}
+
+// Trailing update of one DM block: C <- C - V (T^T (V^T C)) for the n2
+// columns of C, V = the kc <= KW reflectors (unit lower trapezoidal, mloc
+// rows).  V^T C is formed KW x CW at a time (CW = 4096 / KW, 4 x 4 register
+// tiles), T^T applied from shared memory, the result (W2, global scratch
+// [64][n]) subtracted in 64 x 64 tiles.
+template <int KW>
+__device__ void cta_trailing(const double* V0, double* C0, long long lda, int mloc, int kc, int n2, int n,
+                             const double* T, double* g, double* stage, double* W) {
+  constexpr int CW = 4096 / KW;
+  constexpr int NTC = CW / 4;  // threads along the columns
+  constexpr int LV = KW + 1, LC = CW + 1;
+  const int tid = threadIdx.x;
+  const int ta = tid / NTC, tc = tid % NTC;
+  double* sv = stage;
+  double* sc = stage + 32 * LV;
+  auto vat = [&](int r, int q) -> double {
+    return q < kc && r < mloc ? (r > q ? V0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
+  };
+  for (int c0 = 0; c0 < n2; c0 += CW) {
+    double acc[4][4];
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) acc[x][y] = 0.0;
+    for (int r0 = 0; r0 < mloc; r0 += 32) {
+      for (int e = tid; e < 32 * KW; e += blockDim.x) {
+        const int q = e / 32, rr = e % 32;
+        sv[rr * LV + q] = vat(r0 + rr, q);
+      }
+      for (int e = tid; e < 32 * CW; e += blockDim.x) {
+        const int cc = e / 32, rr = e % 32, r = r0 + rr, c = c0 + cc;
+        sc[rr * LC + cc] = (c < n2 && r < mloc) ? C0[(size_t)c * lda + r] : 0.0;
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int rr = 0; rr < 32; ++rr) {
+        double v[4], cv[4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x) v[x] = sv[rr * LV + ta + (KW / 4) * x];
+#pragma unroll
+        for (int y = 0; y < 4; ++y) cv[y] = sc[rr * LC + tc + NTC * y];
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) acc[x][y] = fma(v[x], cv[y], acc[x][y]);
+      }
+      __syncthreads();
+    }
+#pragma unroll
+    for (int x = 0; x < 4; ++x)
+#pragma unroll
+      for (int y = 0; y < 4; ++y) g[(ta + (KW / 4) * x) * LC + tc + NTC * y] = acc[x][y];
+    __syncthreads();
+    // W2 = T^T W (rows aa < kc), to global scratch
+    for (int e = tid; e < KW * CW; e += blockDim.x) {
+      const int aa = e / CW, cc = e % CW;
+      if (c0 + cc >= n2) continue;
+      double s2 = 0.0;
+      if (aa < kc)
+        for (int b = 0; b <= aa; ++b) s2 = fma(T[aa * 64 + b], g[b * LC + cc], s2);
+      W[(size_t)aa * n + c0 + cc] = s2;
+    }
+    __syncthreads();
+    // C -= V W2, 64-row x 64-column tiles (rows fastest across threads)
+    const int tr = tid % 16, tcc = tid / 16;
+    for (int cs = 0; cs < CW && c0 + cs < n2; cs += 64) {
+      const int cb = c0 + cs;
+      for (int r0 = 0; r0 < mloc; r0 += 64) {
+        double u[4][4];
+#pragma unroll
+        for (int x = 0; x < 4; ++x)
+#pragma unroll
+          for (int y = 0; y < 4; ++y) u[x][y] = 0.0;
+        for (int q0 = 0; q0 < kc; q0 += 32) {
+          for (int e = tid; e < 32 * 64; e += blockDim.x) {
+            const int qq = e / 64, rr = e % 64, q = q0 + qq;
+            sv[qq * 65 + rr] = vat(r0 + rr, q);
+            sv[32 * 65 + qq * 65 + rr] = (q < kc && cb + rr < n2) ? W[(size_t)q * n + cb + rr] : 0.0;
+          }
+          __syncthreads();
+#pragma unroll 8
+          for (int qq = 0; qq < 32; ++qq) {
+            double v[4], w[4];
+#pragma unroll
+            for (int x = 0; x < 4; ++x) v[x] = sv[qq * 65 + tr + 16 * x];
+#pragma unroll
+            for (int y = 0; y < 4; ++y) w[y] = sv[32 * 65 + qq * 65 + tcc + 16 * y];
+#pragma unroll
+            for (int x = 0; x < 4; ++x)
+#pragma unroll
+              for (int y = 0; y < 4; ++y) u[x][y] = fma(v[x], w[y], u[x][y]);
+          }
+          __syncthreads();
+        }
+#pragma unroll
+        for (int y = 0; y < 4; ++y) {
+          const int c = cb + tcc + 16 * y;
+          if (c >= n2) continue;
+#pragma unroll
+          for (int x = 0; x < 4; ++x) {
+            const int r = r0 + tr + 16 * x;
+            if (r < mloc) C0[(size_t)c * lda + r] -= u[x][y];
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
 }
 
 struct BatchArgs {
@@ -137,9 +260,24 @@ struct BatchArgs {
   double* ws;          // per-CTA workspace: nrm, nrm_exact, W (64 x nmax)
   long long ws_stride;
   int* queue;
+  unsigned long long* prof;  // per-CTA phase cycles [grid][8] or null
 };
 
-__device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws) {
+// Per-phase cycle accounting (thread 0, after the CTA barrier that ends a
+// phase): 0 norms, 1 selection (sort, Gram, pick, exchanges), 2 panel,
+// 3 T factor, 4 trailing update, 5 downdate / recompute, 6 queue.
+constexpr int kPhases = 8;
+#define BPH(k)                                   \
+  do {                                           \
+    if (tid == 0) {                              \
+      const long long now_ = clock64();          \
+      pacc[(k)] += (unsigned long long)(now_ - pacc[7]); \
+      pacc[7] = (unsigned long long)now_;        \
+    }                                            \
+  } while (0)
+
+__device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
+                          unsigned long long* pacc) {
   const int m = a.m[p], n = a.n[p];
   double* A = a.A + a.a_off[p];
   const long long lda = m;
@@ -187,6 +325,7 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
     S.eta = eta * t;
   }
   __syncthreads();
+  BPH(0);
   if (S.nan) {
     if (tid == 0 && a.info) a.info[p] = -13;
     return;
@@ -228,7 +367,7 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
       auto f = [&](int r, int q) -> double {
         return q < nc ? S.tw[q] * W0[(size_t)S.cand[q].idx * lda + r] : 0.0;
       };
-      cta_gram64(mloc, f, S.stage[0], S.g);
+      cta_gram_any(nc, mloc, f, S.stage, S.g);
     }
     // ---- greedy pick (warp 0) and permute_marked replay (thread 0)
     const int nwords = (nloc + 31) >> 5;
@@ -325,9 +464,9 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
     }
     // whole columns (all m rows), staged `rc` rows at a time through the
     // 2 x 32 x 65-double stage area
-    const int rc = np > 0 ? max(1, min(32, (2 * 32 * 65) / np)) : 1;
+    const int rc = np > 0 ? max(1, min(32, kStage / np)) : 1;
     for (int r0 = 0; r0 < m && np > 0; r0 += rc) {
-      double* st = S.stage[0];
+      double* st = S.stage;
       for (int e = tid; e < np * rc; e += blockDim.x) {
         const int t = e / rc, rr = e % rc, r = r0 + rr;
         if (r < m) st[t * rc + rr] = A[(size_t)(j + S.perm[t].y) * lda + r];
@@ -340,6 +479,7 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
       __syncthreads();
     }
     __syncthreads();
+    BPH(1);
     // ---- panel (dgeqr2_mia) with early exit, columns scaled by 2^-e
     for (int c = tid; c < fjb; c += blockDim.x) S.sc[c] = pow2_for(nrm[j + c]);
     if (tid == 0) {
@@ -414,12 +554,13 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
       }
       __syncthreads();
     }
+    BPH(2);
     // ---- T factor: V^T V then the forward recurrence
     if (kc > 1) {
       auto fv = [&](int r, int q) -> double {
         return q < kc ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
       };
-      cta_gram64(mloc, fv, S.stage[0], S.g);
+      cta_gram_any(kc, mloc, fv, S.stage, S.g);
     }
     for (int e = tid; e < 64 * 64; e += blockDim.x) S.T[e] = 0.0;
     __syncthreads();
@@ -439,99 +580,16 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
         __syncthreads();
       }
     }
+    __syncthreads();
+    BPH(3);
     // ---- trailing update C <- (I - V T V^T)^T C, C = window columns fjb..
     const int n2 = nloc - fjb;
     if (kc > 0 && n2 > 0) {
-      const int ta = tid / 16, tc = tid % 16;
-      for (int c0 = 0; c0 < n2; c0 += 64) {
-        // W = V^T C(:, c0..c0+63)
-        double acc[4][4];
-#pragma unroll
-        for (int x = 0; x < 4; ++x)
-#pragma unroll
-          for (int y = 0; y < 4; ++y) acc[x][y] = 0.0;
-        for (int r0 = 0; r0 < mloc; r0 += 32) {
-          for (int e = tid; e < 32 * 64; e += blockDim.x) {
-            const int q = e / 32, rr = e % 32, r = r0 + rr;
-            const double v = (q < kc && r < mloc) ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
-            S.stage[0][rr * 65 + q] = v;
-            const int c = c0 + q;
-            S.stage[1][rr * 65 + q] = (c < n2 && r < mloc) ? W0[(size_t)(fjb + c) * lda + r] : 0.0;
-          }
-          __syncthreads();
-#pragma unroll 4
-          for (int rr = 0; rr < 32; ++rr) {
-            double v[4], cv[4];
-#pragma unroll
-            for (int x = 0; x < 4; ++x) v[x] = S.stage[0][rr * 65 + ta + 16 * x];
-#pragma unroll
-            for (int y = 0; y < 4; ++y) cv[y] = S.stage[1][rr * 65 + tc + 16 * y];
-#pragma unroll
-            for (int x = 0; x < 4; ++x)
-#pragma unroll
-              for (int y = 0; y < 4; ++y) acc[x][y] = fma(v[x], cv[y], acc[x][y]);
-          }
-          __syncthreads();
-        }
-#pragma unroll
-        for (int x = 0; x < 4; ++x)
-#pragma unroll
-          for (int y = 0; y < 4; ++y) S.g[(ta + 16 * x) * 65 + tc + 16 * y] = acc[x][y];
-        __syncthreads();
-        // W2 = T^T W  -> stage[1] as [a][c]
-        for (int e = tid; e < 64 * 64; e += blockDim.x) {
-          const int aa = e / 64, cc = e % 64;
-          double s2 = 0.0;
-          if (aa < kc)
-            for (int b = 0; b <= aa; ++b) s2 = fma(S.T[aa * 64 + b], S.g[b * 65 + cc], s2);
-          if (c0 + cc < n2) W[(size_t)aa * n + c0 + cc] = s2;
-        }
-        __syncthreads();
-        // C -= V W2, 64-row tiles (rows fastest across threads)
-        const int tr = tid % 16, tcc = tid / 16;
-        for (int r0 = 0; r0 < mloc; r0 += 64) {
-          double u[4][4];
-#pragma unroll
-          for (int x = 0; x < 4; ++x)
-#pragma unroll
-            for (int y = 0; y < 4; ++y) u[x][y] = 0.0;
-          for (int q0 = 0; q0 < kc; q0 += 32) {
-            for (int e = tid; e < 32 * 64; e += blockDim.x) {
-              const int qq = e / 64, rr = e % 64, q = q0 + qq, r = r0 + rr;
-              S.stage[0][qq * 65 + rr] =
-                  (q < kc && r < mloc) ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
-              const int cc = rr;
-              S.stage[1][qq * 65 + cc] = (q < kc && c0 + cc < n2) ? W[(size_t)q * n + c0 + cc] : 0.0;
-            }
-            __syncthreads();
-#pragma unroll 8
-            for (int qq = 0; qq < 32; ++qq) {
-              double v[4], w[4];
-#pragma unroll
-              for (int x = 0; x < 4; ++x) v[x] = S.stage[0][qq * 65 + tr + 16 * x];
-#pragma unroll
-              for (int y = 0; y < 4; ++y) w[y] = S.stage[1][qq * 65 + tcc + 16 * y];
-#pragma unroll
-              for (int x = 0; x < 4; ++x)
-#pragma unroll
-                for (int y = 0; y < 4; ++y) u[x][y] = fma(v[x], w[y], u[x][y]);
-            }
-            __syncthreads();
-          }
-#pragma unroll
-          for (int y = 0; y < 4; ++y) {
-            const int c = c0 + tcc + 16 * y;
-            if (c >= n2) continue;
-#pragma unroll
-            for (int x = 0; x < 4; ++x) {
-              const int r = r0 + tr + 16 * x;
-              if (r < mloc) W0[(size_t)(fjb + c) * lda + r] -= u[x][y];
-            }
-          }
-        }
-        __syncthreads();
-      }
+      if (kc <= 32) cta_trailing<32>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, S.g, S.stage, W);
+      else cta_trailing<64>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, S.g, S.stage, W);
     }
+    __syncthreads();
+    BPH(4);
     // ---- partial-norm downdate (norm_update) and recomputes
     if (tid == 0) {
       S.nlist = 0;
@@ -582,6 +640,7 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws)
       ncols[it] = kc;
     }
     __syncthreads();
+    BPH(5);
     ++it;
     j += kc;
     if (S.stop_mode >= 1 && S.stop_mode <= 3) {
@@ -596,18 +655,28 @@ __global__ void __launch_bounds__(BT, 1) k_dmqr_batched(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BatchShared& S = *reinterpret_cast<BatchShared*>(smem_raw);
   double* ws = a.ws + (size_t)blockIdx.x * a.ws_stride;
+  const int tid = threadIdx.x;
+  unsigned long long pacc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0};
+  const long long t0 = clock64();
+  pacc[7] = (unsigned long long)t0;
   while (true) {
     if (threadIdx.x == 0) S.next = atomicAdd(a.queue, 1);
     __syncthreads();
     const int q = S.next;
     __syncthreads();
+    BPH(6);
     if (q >= a.count) break;
-    solve_one(a, a.order[q], S, ws);
+    solve_one(a, a.order[q], S, ws, pacc);
     __syncthreads();
+  }
+  if (a.prof && tid == 0) {
+    for (int k = 0; k < 7; ++k) a.prof[(size_t)blockIdx.x * kPhases + k] = pacc[k];
+    a.prof[(size_t)blockIdx.x * kPhases + 7] = (unsigned long long)(clock64() - t0);
   }
 }
 
 size_t batched_smem_bytes() { return sizeof(BatchShared); }
+int batched_phases() { return kPhases; }
 int batched_nmax() { return BNMAX; }
 int batched_kmax() { return BKMAX; }
 long long batched_ws_doubles(int nmax) { return 2LL * BNMAX + 64LL * nmax; }
@@ -640,6 +709,7 @@ int launch_batched(const BatchLaunch& L, cudaStream_t s) {
   a.ws = L.ws;
   a.ws_stride = L.ws_stride;
   a.queue = L.queue;
+  a.prof = L.prof;
   if (cudaMemsetAsync(L.queue, 0, sizeof(int), s) != cudaSuccess) return 1;
   k_dmqr_batched<<<L.grid, BT, sizeof(BatchShared), s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;

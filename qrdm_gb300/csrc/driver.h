@@ -52,7 +52,7 @@ struct Ctx {
   Buf pan_part, pan_row, pan_bar, vtv_part, vtv, T, wpart, w2;
   Buf qF, qg, qpart, qst;
   Buf oz_va2, oz_vb1, oz_wb2, oz_wexp, oz_wp;  // mixed-precision trailing update
-  Buf b_meta, b_ws;                             // batched DM-QR
+  Buf b_meta, b_ws, b_prof;                     // batched DM-QR
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch
   unsigned long long b_key = 0;
   BlockState* h_st = nullptr;              // pinned host copy of the block record

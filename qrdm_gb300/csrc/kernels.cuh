@@ -118,9 +118,11 @@ struct BatchLaunch {
   double* ws;
   long long ws_stride;
   int* queue;
+  unsigned long long* prof;
   int grid;
 };
 int batched_set_attributes();
+int batched_phases();
 int launch_batched(const BatchLaunch& L, cudaStream_t s);
 size_t batched_smem_bytes();
 int batched_nmax();
