@@ -34,7 +34,6 @@
 namespace qrdm {
 
 constexpr int OZ_TPB = 256;
-constexpr int OZ_MAXS = 8;
 
 // round(x * 2^sh) as int64 (|result| < 2^62 by the caller's choice of sh)
 __device__ __forceinline__ long long fixed_point(double x, int sh) {
@@ -59,18 +58,20 @@ __device__ __forceinline__ long long fixed_point(double x, int sh) {
   return (b >> 63) ? -F : F;
 }
 
-// s balanced base-256 digits of F (d[0] most significant), |d| <= 128.
-__device__ __forceinline__ void balanced_digits(long long F, int s, int* d) {
+// S balanced base-256 digits of F (d[0] most significant; the lower ones in
+// [-128, 127]).  Adding 128 at every lower digit position makes those digits
+// plain bytes of G = F + bias (no carries), so each is one byte extract:
+// d = byte - 128; the top digit is G >> 8 (S - 1).
+template <int S>
+__device__ __forceinline__ void balanced_digits(long long F, int* d) {
+  const long long G = F + (long long)(0x8080808080808080ull >> (8 * (9 - S)));
+  const uint32_t lo = (uint32_t)G, hi = (uint32_t)((unsigned long long)G >> 32);
 #pragma unroll
-  for (int p = OZ_MAXS - 1; p >= 1; --p) {
-    if (p < s) {
-      int r = (int)(F & 255);
-      if (r >= 128) r -= 256;
-      d[p] = r;
-      F = (F - r) >> 8;
-    }
+  for (int b = 0; b < S - 1; ++b) {  // byte b from the bottom = digit S-1-b
+    const uint32_t word = b < 4 ? lo : hi;
+    d[S - 1 - b] = (int)((word >> (8 * (b & 3))) & 255u) - 128;
   }
-  d[0] = (int)F;
+  d[0] = (int)(G >> (8 * (S - 1)));
 }
 
 // |d| <= 256 integer -> FP32 exactly via the 1.5 * 2^23 shifter (one integer
@@ -104,8 +105,9 @@ __device__ __forceinline__ int scale_exp_of(double bound) {
 //   va2[t][p]: rows 128t..128t+127, K = the 64 reflector columns (GEMM2 A)
 //   vb1[b][p]: N = the 64 reflector columns, K = rows 64b..64b+63 (GEMM1 B)
 // fixed scale 2^1.  One thread per (row, pair of reflector columns).
-__global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict__ V, long long ldv,
-                                                        int mloc, int s, const BlockState* __restrict__ st,
+template <int S>
+__global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict__ V, long long ldv, int mloc,
+                                                        const BlockState* __restrict__ st,
                                                         unsigned char* __restrict__ va2,
                                                         unsigned char* __restrict__ vb1) {
   const int k = st->fjb_cmp;
@@ -113,26 +115,28 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict_
   const int mpad = ceil_div(mloc, 256) * 256;
   if (e >= (long long)mpad * 32) return;
   const int r = (int)(e / 32), ap = (int)(e % 32);  // row, column pair
-  const int sh = 8 * s - 1;
-  int dg[2][OZ_MAXS];
+  const int sh = 8 * S - 1;
+  int dg[2][S];
 #pragma unroll
   for (int h = 0; h < 2; ++h) {
     const int a = 2 * ap + h;
     double v = 0.0;
     if (r < mloc && a < k) v = r > a ? V[(size_t)a * ldv + r] : (r == a ? 1.0 : 0.0);
-    balanced_digits(fixed_point(v, sh), s, dg[h]);
+    balanced_digits<S>(fixed_point(v, sh), dg[h]);
   }
   const int t = r >> 7, rr = r & 127;
-  for (int p = 0; p < s; ++p) {
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
     // GEMM2 A tile: row rr, K = a (pair packed)
-    unsigned char* ta = va2 + ((size_t)t * s + p) * 16384;
+    unsigned char* ta = va2 + ((size_t)t * S + p) * 16384;
     *reinterpret_cast<uint32_t*>(ta + tc::sw128_offset(rr, 2 * ap)) = pack2_bf16(dg[0][p], dg[1][p]);
   }
   // GEMM1 B tile: row (N) = a, K = r % 64 -- the two reflector columns land in
   // different rows; store 16-bit values
   const int b = r >> 6, kr = r & 63;
-  for (int p = 0; p < s; ++p) {
-    unsigned char* tb = vb1 + ((size_t)b * s + p) * 8192;
+#pragma unroll
+  for (int p = 0; p < S; ++p) {
+    unsigned char* tb = vb1 + ((size_t)b * S + p) * 8192;
 #pragma unroll
     for (int h = 0; h < 2; ++h)
       *reinterpret_cast<unsigned short*>(tb + tc::sw128_offset(2 * ap + h, kr)) = bf16_bits(dg[h][p]);
@@ -140,38 +144,43 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict_
 }
 
 // ------------------------------------------------------- shared helpers
-// Issue the digit-pair MMAs of one 64-deep K block: A digits at a_tiles
-// (s tiles of 128 x 64, stride a_stride), B digits stacked at b_tiles
-// (s tiles of 64 rows, 8 KB each); level L = p + q (1-based digits) lands in
-// TMEM columns (L - 2) * 64.  first: overwrite instead of accumulate.
+// Issue the digit-pair MMAs of the K16 steps [kk0, kk1) of one 64-deep K
+// block: A digits at a_tiles (S tiles of 128 x 64, stride a_stride), B digits
+// stacked at b_tiles (S tiles of 64 rows, 8 KB each); level L = p + q
+// (1-based digits) lands in TMEM columns (L - 2) * 64.  first: the first
+// step overwrites instead of accumulating (digit p = 1 covers every level).
+template <int S>
 __device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32_t a_stride, uint32_t b_tiles,
-                                         int s, bool first) {
-  for (int p = 1; p <= s; ++p) {
-    const int Q = s + 1 - p;  // q = 1..Q
+                                         int kk0, int kk1, bool first) {
+#pragma unroll
+  for (int p = 1; p <= S; ++p) {
+    const int Q = S + 1 - p;  // q = 1..Q
+#pragma unroll
     for (int q0 = 1; q0 <= Q; q0 += 4) {
       const int nq = min(4, Q - q0 + 1);
       const uint32_t idesc = tc::idesc_bf16_f32(128, 64 * nq);
       const uint32_t dcol = (uint32_t)((p + q0 - 2) * 64);
-      for (int kk = 0; kk < 4; ++kk) {
+      for (int kk = kk0; kk < kk1; ++kk) {
         uint64_t ad = tc::desc_sw128(a_tiles + (uint32_t)(p - 1) * a_stride + kk * 32);
         uint64_t bd = tc::desc_sw128(b_tiles + (uint32_t)(q0 - 1) * 8192u + kk * 32);
-        tc::mma_bf16(tmem + dcol, ad, bd, idesc, (first && p == 1 && kk == 0) ? 0u : 1u);
+        tc::mma_bf16(tmem + dcol, ad, bd, idesc, (first && p == 1 && kk == kk0) ? 0u : 1u);
       }
     }
   }
 }
 
-// Load the s levels of 8 accumulator columns (col0..col0+7) of this thread's
+// Load the S levels of 8 accumulator columns (col0..col0+7) of this thread's
 // TMEM lane and combine them: hi = sum_{L<=5} D_L 2^(8(5-L)) (exact int64),
-// mid = sum_{L>=6} D_L 2^(8(s+1-L)) (int64 of exact or nearly exact values).
-__device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, int s, long long* hi,
-                                           long long* mid) {
+// mid = sum_{L>=6} D_L 2^(8(S+1-L)) (int64 of exact or nearly exact values).
+template <int S>
+__device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long long* hi, long long* mid) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     hi[i] = 0;
     mid[i] = 0;
   }
-  for (int L = 2; L <= s + 1; ++L) {
+#pragma unroll
+  for (int L = 2; L <= S + 1; ++L) {
     uint32_t r[8];
     asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
                  : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
@@ -183,7 +192,7 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, int s,
     for (int i = 0; i < 8; ++i) {
       long long v = (long long)f32_to_int(__uint_as_float(r[i]));
       if (L <= 5) hi[i] += v << (8 * (5 - L));
-      else mid[i] += v << (8 * (s + 1 - L));
+      else mid[i] += v << (8 * (S + 1 - L));
     }
   }
 }
@@ -192,26 +201,34 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, int s,
 // Partial W^T tile: 128 columns of C x the k (<= 64) reflector columns,
 // over the 256-row chunks [chunk_begin, chunk_end) of the window.
 // Wp[split][c][a] (FP64).  C columns start at window column st->fjb.
+//
+// Pipeline per 64-row block: the C digits (A operand, converted from FP64 by
+// all threads) are written half a block (32 rows = K16 steps 2h, 2h+1) at a
+// time, so converting one half overlaps the tensor core's work on the other;
+// each half's MMAs commit to their own mbarrier, which frees that half.  The
+// V digits (B operand) of the next block arrive by one bulk copy into the
+// second of two buffers.  C loads for the next half are issued before the
+// current half's digits are stored.
 struct OzG1Args {
   const double* W0;     // window origin A(j, j)
   long long lda;
   int mloc, ncols;      // window rows / columns
   const double* nrm;    // partial norms, window-relative
   const unsigned char* vb1;
-  int s;
   int chunks_per_split;
   double* Wp;           // [split][npad][64]
   int npad;
   BlockState* st;
 };
 
+template <int S>
 __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const int s = g.s;
-  unsigned char* adig = base;                  // s x 16 KB
-  unsigned char* bdig = base + s * 16384;      // s x 8 KB
-  __shared__ uint64_t bar;
+  unsigned char* adig = base;               // S x 16 KB: 128 C columns x 64 rows
+  unsigned char* bdig = base + S * 16384;   // 2 x S x 8 KB: 64 reflectors x 64 rows
+  constexpr uint32_t BBYTES = S * 8192;
+  __shared__ uint64_t abar[2], bfull[2];
   __shared__ uint32_t s_tmem;
   __shared__ int s_e[128];
   const int fjb = g.st->fjb;
@@ -221,14 +238,22 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
   const int nchunk = ceil_div(g.mloc, 256);
   const int ch_begin = blockIdx.y * g.chunks_per_split;
   const int ch_end = min(nchunk, ch_begin + g.chunks_per_split);
+  const int nblk = 4 * max(0, ch_end - ch_begin);
   const int tid = threadIdx.x;
   if (tid < 128) {
     const int c = c0 + tid;
     s_e[tid] = c < g.ncols ? scale_exp_of(g.nrm[c]) : 0;
   }
   if (tid == 0) {
-    tc::mbar_init(&bar, 1);
+    tc::mbar_init(&abar[0], 1);
+    tc::mbar_init(&abar[1], 1);
+    tc::mbar_init(&bfull[0], 1);
+    tc::mbar_init(&bfull[1], 1);
     tc::fence_mbar_init();
+    if (nblk > 0) {
+      tc::mbar_arrive_expect_tx(&bfull[0], BBYTES);
+      tc::bulk_g2s(bdig, g.vb1 + (size_t)(ch_begin * 4) * BBYTES, BBYTES, &bfull[0]);
+    }
   }
   if (tid < 32) tc::tmem_alloc(&s_tmem, 512);
   tc::fence_before_sync();
@@ -246,85 +271,131 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
     acc_hi[i] = 0;
     acc_mid[i] = 0.f;
   }
-  uint32_t phase = 0;
-  bool ok = true;
-  for (int ch = ch_begin; ch < ch_end && ok; ++ch) {
-    for (int kb = 0; kb < 4; ++kb) {
-      const int r0 = ch * 256 + kb * 64;
-      // C rows r0..r0+63 x columns c0..c0+127 -> A digit tiles (row = column of C)
-      // 16 row pairs per thread, loaded 4 at a time before any conversion so
-      // the global loads overlap (the conversion is latency-bound otherwise)
-#pragma unroll 1
-      for (int it = 0; it < 16; it += 4) {
-        double2 xv[4];
+  // C rows r0 + 32 h + [0, 32) x columns c0 + [0, 128): 8 row pairs per thread,
+  // 16 consecutive threads on one column (256 contiguous bytes)
+  double2 xv[8];
+  auto load_half = [&](int ib, int h) {
+    const int rb = (ch_begin + (ib >> 2)) * 256 + (ib & 3) * 64 + 32 * h;
 #pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int e = tid + OZ_TPB * (it + u);
-          const int rp = e & 31, cc = e >> 5;
-          const int c = c0 + cc, r = r0 + 2 * rp;
-          xv[u] = make_double2(0.0, 0.0);
-          if (c < g.ncols) {
-            const double* col = g.W0 + (size_t)c * g.lda;
-            if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
-              xv[u] = __ldg(reinterpret_cast<const double2*>(col + r));
-            } else {
-              if (r < g.mloc) xv[u].x = __ldg(col + r);
-              if (r + 1 < g.mloc) xv[u].y = __ldg(col + r + 1);
-            }
-          }
-        }
-#pragma unroll
-        for (int u = 0; u < 4; ++u) {
-          const int e = tid + OZ_TPB * (it + u);
-          const int rp = e & 31, cc = e >> 5;
-          const int sh = 8 * s - s_e[cc];
-          int d0[OZ_MAXS], d1[OZ_MAXS];
-          balanced_digits(fixed_point(xv[u].x, sh), s, d0);
-          balanced_digits(fixed_point(xv[u].y, sh), s, d1);
-          const uint32_t off = tc::sw128_offset(cc, 2 * rp);
-#pragma unroll
-          for (int p = 0; p < OZ_MAXS; ++p)
-            if (p < s) *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+    for (int u = 0; u < 8; ++u) {
+      const int e = tid + OZ_TPB * u;
+      const int rp = e & 15, cc = e >> 4;
+      const int c = c0 + cc, r = rb + 2 * rp;
+      double2 x = make_double2(0.0, 0.0);
+      if (c < g.ncols) {
+        const double* col = g.W0 + (size_t)c * g.lda;
+        if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
+          x = __ldg(reinterpret_cast<const double2*>(col + r));
+        } else {
+          if (r < g.mloc) x.x = __ldg(col + r);
+          if (r + 1 < g.mloc) x.y = __ldg(col + r + 1);
         }
       }
-      // V digits of this 64-row block (GEMM1 B tiles, contiguous s x 8 KB)
-      {
-        const int b = r0 >> 6;
-        const uint4* src = reinterpret_cast<const uint4*>(g.vb1 + (size_t)b * s * 8192);
-        uint4* dst = reinterpret_cast<uint4*>(bdig);
-        for (int e = tid; e < s * 512; e += OZ_TPB) dst[e] = src[e];
+      xv[u] = x;
+    }
+  };
+  if (nblk > 0) load_half(0, 0);
+  // failures (a bounded wait that gave up) are per thread and combined at
+  // the next barrier with __syncthreads_or, so every thread leaves together
+  uint32_t aph[2] = {0u, 0u}, bpar[2] = {0u, 0u};
+  bool apend[2] = {false, false};
+  bool bpend[2] = {nblk > 0, false};
+  bool lf = false, ok = true;
+  for (int ib = 0; ib < nblk && ok; ++ib) {
+    const int kb = ib & 3;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      // the MMAs that read half h of the A tile (and, for h = 1, every MMA of
+      // the previous block, hence the other B buffer) must be complete
+      if (apend[h]) {
+        if (!tc::mbar_wait(&abar[h], aph[h])) lf = true;
+        aph[h] ^= 1u;
+        apend[h] = false;
       }
+      if (h == 1 && ib + 1 < nblk) {
+        const int nb = (ib + 1) & 1;
+        if (tid == 0) {
+          tc::mbar_arrive_expect_tx(&bfull[nb], BBYTES);
+          tc::bulk_g2s(bdig + nb * BBYTES, g.vb1 + (size_t)(ch_begin * 4 + ib + 1) * BBYTES, BBYTES,
+                       &bfull[nb]);
+        }
+        bpend[nb] = true;
+        bpar[nb] = (uint32_t)(((ib + 1) >> 1) & 1);
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = tid + OZ_TPB * u;
+        const int rp = e & 15, cc = e >> 4;
+        const int sh = 8 * S - s_e[cc];
+        int d0[S], d1[S];
+        balanced_digits<S>(fixed_point(xv[u].x, sh), d0);
+        balanced_digits<S>(fixed_point(xv[u].y, sh), d1);
+        const uint32_t off = tc::sw128_offset(cc, 32 * h + 2 * rp);
+#pragma unroll
+        for (int p = 0; p < S; ++p)
+          *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+      }
+      // C of the next half, in flight while this half is multiplied
+      if (h == 0) load_half(ib, 1);
+      else if (ib + 1 < nblk) load_half(ib + 1, 0);
       tc::fence_async_smem();
-      __syncthreads();
+      if (__syncthreads_or(lf)) {
+        ok = false;
+        break;
+      }
       if (tid == 0) {
         tc::fence_after_sync();
-        oz_issue(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig), s, kb == 0);
-        tc::mma_commit(&bar);
+        bool ready = true;
+        if (h == 0) {
+          ready = tc::mbar_wait(&bfull[ib & 1], bpar[ib & 1]);
+          if (!ready) lf = true;
+        }
+        if (ready)
+          oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig + (ib & 1) * BBYTES), 2 * h, 2 * h + 2,
+                      kb == 0 && h == 0);
+        tc::mma_commit(&abar[h]);
       }
-      if (!tc::mbar_wait(&bar, phase)) {
-        atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
-        ok = false;
-      }
-      phase ^= 1u;
-      tc::fence_after_sync();
+      if (h == 0) bpend[ib & 1] = false;
+      apend[h] = true;
     }
     if (!ok) break;
-    // drain the chunk's levels into the integer accumulators
+    if (kb == 3 || ib == nblk - 1) {
+      // end of a 256-row chunk: drain the levels into the integer accumulators
 #pragma unroll
-    for (int g8 = 0; g8 < 4; ++g8) {
-      long long hi[8], mid[8];
-      oz_levels8(taddr, 32 * half + 8 * g8, s, hi, mid);
+      for (int h = 0; h < 2; ++h)
+        if (apend[h]) {
+          if (!tc::mbar_wait(&abar[h], aph[h])) lf = true;
+          aph[h] ^= 1u;
+          apend[h] = false;
+        }
+      tc::fence_after_sync();
 #pragma unroll
-      for (int i = 0; i < 8; ++i) {
-        acc_hi[8 * g8 + i] += hi[i];
-        acc_mid[8 * g8 + i] += (float)mid[i];
+      for (int g8 = 0; g8 < 4; ++g8) {
+        long long hi[8], mid[8];
+        oz_levels8<S>(taddr, 32 * half + 8 * g8, hi, mid);
+#pragma unroll
+        for (int i = 0; i < 8; ++i) {
+          acc_hi[8 * g8 + i] += hi[i];
+          acc_mid[8 * g8 + i] += (float)mid[i];
+        }
       }
+      tc::fence_before_sync();
+      if (__syncthreads_or(lf)) ok = false;
     }
-    tc::fence_before_sync();
-    __syncthreads();
   }
-  // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(s+1))
-  if (ok) {
+  // on failure: let the commits and copies still in flight land before the
+  // shared memory and TMEM are released (bounded waits)
+#pragma unroll
+  for (int h = 0; h < 2; ++h)
+    if (apend[h]) tc::mbar_wait(&abar[h], aph[h]);
+  if (tid == 0) {
+    for (int b = 0; b < 2; ++b)
+      if (bpend[b]) tc::mbar_wait(&bfull[b], bpar[b]);
+  }
+  if (!ok) {
+    if (tid == 0) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+  } else {
+    // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1))
     const int c = c0 + row;
     double* out = g.Wp + ((size_t)blockIdx.y * g.npad + (size_t)(c - fjb)) * 64;
     if (c < g.ncols) {
@@ -332,7 +403,7 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
 #pragma unroll
       for (int i = 0; i < 32; ++i) {
         const int a = 32 * half + i;
-        double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (s + 1)));
+        double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
         out[a] = a < k ? v : 0.0;
       }
     }
@@ -344,14 +415,15 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
 
 // ------------------------------------------- W2 = T^T W and its digits
 // One CTA per 16 C-columns (a quarter of a 64-row GEMM2 B tile): sum the
-// split partials (fixed order), apply T^T, then slice W2 per column (scale
-// 2^(E+1) of the column max) into the GEMM2 B tiles wb2[tile][q]
-// (N = C column, K = reflector column).
+// split partials (fixed order, eight loads in flight), apply T^T, then slice
+// W2 per column (scale 2^(E+1) of the column max) into the GEMM2 B tiles
+// wb2[tile][q] (N = C column, K = reflector column).
 constexpr int OZ_W2_COLS = 16;
 
+template <int S>
 __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp, int nsplit, int npad,
                                                    const double* __restrict__ T, int ldt, int ncols,
-                                                   int s, const BlockState* __restrict__ st,
+                                                   const BlockState* __restrict__ st,
                                                    unsigned char* __restrict__ wb2, int* __restrict__ wexp) {
   __shared__ double sW[OZ_W2_COLS][65];  // [c][a]
   __shared__ double sT[64][65];          // T(b, a) at [a][b]
@@ -360,13 +432,26 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
   const int ncols_c = ncols - st->fjb;  // columns of C
   const int cbase = blockIdx.x * OZ_W2_COLS;
   if (cbase >= ncols_c || k <= 0) return;
+  const size_t sstride = (size_t)npad * 64;
+#pragma unroll 1
   for (int e = threadIdx.x; e < OZ_W2_COLS * 64; e += blockDim.x) {
     const int cc = e / 64, a = e % 64;
     double acc = 0.0;
-    if (a < k && cbase + cc < ncols_c)
-      for (int q = 0; q < nsplit; ++q) acc += Wp[((size_t)q * npad + cbase + cc) * 64 + a];
+    if (a < k && cbase + cc < ncols_c) {
+      const double* src = Wp + (size_t)(cbase + cc) * 64 + a;
+      int q = 0;
+      for (; q + 8 <= nsplit; q += 8) {
+        double v[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(src + (size_t)(q + u) * sstride);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc += v[u];
+      }
+      for (; q < nsplit; ++q) acc += __ldcg(src + (size_t)q * sstride);
+    }
     sW[cc][a] = acc;
   }
+#pragma unroll 4
   for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
     const int a = e / 64, b = e % 64;
     sT[a][b] = (a < k && b < k) ? T[(size_t)a * ldt + b] : 0.0;
@@ -401,21 +486,21 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
   const int tile = cbase / 64, row0 = cbase % 64;
   for (int e = threadIdx.x; e < OZ_W2_COLS * 32; e += blockDim.x) {
     const int cc = e / 32, ap = e % 32;
-    const int sh = 8 * s - scale_exp_of(smax[cc]);
-    int d0[OZ_MAXS], d1[OZ_MAXS];
-    balanced_digits(fixed_point(sW[cc][2 * ap], sh), s, d0);
-    balanced_digits(fixed_point(sW[cc][2 * ap + 1], sh), s, d1);
+    const int sh = 8 * S - scale_exp_of(smax[cc]);
+    int d0[S], d1[S];
+    balanced_digits<S>(fixed_point(sW[cc][2 * ap], sh), d0);
+    balanced_digits<S>(fixed_point(sW[cc][2 * ap + 1], sh), d1);
     const uint32_t off = tc::sw128_offset(row0 + cc, 2 * ap);
 #pragma unroll
-    for (int q = 0; q < OZ_MAXS; ++q)
-      if (q < s)
-        *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * s + q) * 8192 + off) = pack2_bf16(d0[q], d1[q]);
+    for (int q = 0; q < S; ++q)
+      *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * S + q) * 8192 + off) = pack2_bf16(d0[q], d1[q]);
   }
 }
 
 // ------------------------------------------------------------- GEMM 2
 // C(r, c) -= V(r, :) W2(:, c) for a 128-row x 64-column tile of C
-// (C columns start at window column st->fjb).
+// (C columns start at window column st->fjb).  Both digit operands arrive by
+// bulk copies; the tile's C entries are loaded while the tensor core works.
 struct OzG2Args {
   double* W0;
   long long lda;
@@ -423,37 +508,31 @@ struct OzG2Args {
   const unsigned char* va2;
   const unsigned char* wb2;
   const int* wexp;
-  int s;
   BlockState* st;
 };
 
-
+template <int S>
 __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const int s = g.s;
-  unsigned char* adig = base;              // s x 16 KB
-  unsigned char* bdig = base + s * 16384;  // s x 8 KB
-  __shared__ uint64_t bar;
+  unsigned char* adig = base;              // S x 16 KB
+  unsigned char* bdig = base + S * 16384;  // S x 8 KB
+  __shared__ uint64_t bar, lbar;
   __shared__ uint32_t s_tmem;
+  __shared__ int s_ok;
   const int fjb = g.st->fjb;
   const int k = g.st->fjb_cmp;
   const int ct = blockIdx.x, rt = blockIdx.y;
   const int cw0 = ct * 64;  // first C column relative to fjb
   if (fjb + cw0 >= g.ncols || rt * 128 >= g.mloc || k <= 0) return;
   const int tid = threadIdx.x;
-  {
-    const uint4* sa = reinterpret_cast<const uint4*>(g.va2 + (size_t)rt * s * 16384);
-    uint4* da = reinterpret_cast<uint4*>(adig);
-    for (int e = tid; e < s * 1024; e += OZ_TPB) da[e] = sa[e];
-    const uint4* sb = reinterpret_cast<const uint4*>(g.wb2 + (size_t)ct * s * 8192);
-    uint4* db = reinterpret_cast<uint4*>(bdig);
-    for (int e = tid; e < s * 512; e += OZ_TPB) db[e] = sb[e];
-  }
-  tc::fence_async_smem();
   if (tid == 0) {
     tc::mbar_init(&bar, 1);
+    tc::mbar_init(&lbar, 1);
     tc::fence_mbar_init();
+    tc::mbar_arrive_expect_tx(&lbar, S * (16384 + 8192));
+    tc::bulk_g2s(adig, g.va2 + (size_t)rt * S * 16384, S * 16384, &lbar);
+    tc::bulk_g2s(bdig, g.wb2 + (size_t)ct * S * 8192, S * 8192, &lbar);
   }
   if (tid < 32) tc::tmem_alloc(&s_tmem, 512);
   tc::fence_before_sync();
@@ -461,8 +540,10 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
   if (tid == 0) {
-    oz_issue(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig), s, true);
+    const bool loaded = tc::mbar_wait(&lbar, 0);
+    if (loaded) oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig), 0, 4, true);
     tc::mma_commit(&bar);
+    s_ok = loaded ? 1 : 0;
   }
   const int w = tid >> 5, lane = tid & 31;
   const int rr = 32 * (w & 3) + lane;
@@ -476,14 +557,16 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
     const int c = fjb + cw0 + 32 * half + i;
     cv[i] = (r < g.mloc && c < g.ncols) ? g.W0[(size_t)c * g.lda + r] : 0.0;
   }
-  const bool ok = tc::mbar_wait(&bar, 0);
-  if (!ok) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+  bool ok = tc::mbar_wait(&bar, 0);
+  __syncthreads();
+  ok = ok && s_ok;
+  if (!ok && tid == 0) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
   tc::fence_after_sync();
   if (ok) {
 #pragma unroll
     for (int g8 = 0; g8 < 4; ++g8) {
       long long hi[8], mid[8];
-      oz_levels8(taddr, 32 * half + 8 * g8, s, hi, mid);
+      oz_levels8<S>(taddr, 32 * half + 8 * g8, hi, mid);
       if (r < g.mloc) {
 #pragma unroll
         for (int i = 0; i < 8; ++i) {
@@ -491,10 +574,10 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
           const int c = fjb + cw;
           if (c < g.ncols) {
             const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
-            // U = 2^e (hi 256^-5 + mid 256^-(s+1)).  hi < 2^45 and
-            // mid < 2^40, so hi 2^17 + mid 2^(57-8s) fits in 62 bits and keeps
+            // U = 2^e (hi 256^-5 + mid 256^-(S+1)).  hi < 2^45 and
+            // mid < 2^40, so hi 2^17 + mid 2^(57-8S) fits in 62 bits and keeps
             // ~2^-62 of U: one conversion, one FP64 subtraction.
-            const int msh = 8 * (s + 1) - 40 - 17;  // weight of mid relative to hi 2^17
+            constexpr int msh = 8 * (S + 1) - 40 - 17;  // weight of mid relative to hi 2^17
             const long long comb = (hi[i] << 17) + (msh >= 0 ? (mid[i] >> msh) : (mid[i] << -msh));
             const double u = (double)comb * pow2d(e - 40 - 17);
             g.W0[(size_t)c * g.lda + r] = cv[8 * g8 + i] - u;
@@ -509,25 +592,32 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
 }
 
 // ------------------------------------------------------------ launchers
-size_t oz_gemm_smem(int s) { return (size_t)s * (16384 + 8192) + 1024; }
+static size_t oz_gemm1_smem(int s) { return (size_t)s * (16384 + 2 * 8192) + 1024; }
+static size_t oz_gemm2_smem(int s) { return (size_t)s * (16384 + 8192) + 1024; }
+size_t oz_gemm_smem(int s) { return oz_gemm1_smem(s); }
 
-int oz_set_attributes() {
-  const int bytes = (int)oz_gemm_smem(OZ_MAXS);
-  if (cudaFuncSetAttribute(k_oz_gemm1, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+template <int S>
+static int oz_set_attributes_s() {
+  if (cudaFuncSetAttribute(k_oz_gemm1<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_gemm1_smem(S)) !=
+      cudaSuccess)
     return 1;
-  if (cudaFuncSetAttribute(k_oz_gemm2, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess)
+  if (cudaFuncSetAttribute(k_oz_gemm2<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_gemm2_smem(S)) !=
+      cudaSuccess)
     return 1;
   return 0;
 }
 
-// Whole mixed-precision trailing update of one DM block.  Buffers: va2/vb1
-// (V digits), wb2 (W2 digits), wexp (n ints), Wp (nsplit x npad x 64 FP64).
-int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
-                       const double* T, int ldt, int s, int nsm, BlockState* st, unsigned char* va2,
-                       unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp, int* launches) {
-  if (ncols <= 1 || mloc <= 0) return 0;
+int oz_set_attributes() {
+  return oz_set_attributes_s<4>() | oz_set_attributes_s<5>() | oz_set_attributes_s<6>() |
+         oz_set_attributes_s<7>();
+}
+
+template <int S>
+static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
+                  const double* T, int ldt, int nsm, BlockState* st, unsigned char* va2, unsigned char* vb1,
+                  unsigned char* wb2, int* wexp, double* Wp) {
   const int mpad = ceil_div(mloc, 256) * 256;
-  k_oz_slice_v<<<ceil_div(mpad * 32, OZ_TPB), OZ_TPB, 0, st_>>>(W0, lda, mloc, s, st, va2, vb1);
+  k_oz_slice_v<S><<<ceil_div(mpad * 32, OZ_TPB), OZ_TPB, 0, st_>>>(W0, lda, mloc, st, va2, vb1);
   const int ctiles = ceil_div(ncols - 1, 128);  // >= 1 column is selected
   const int nchunk = ceil_div(mloc, 256);
   int nsplit = std::max(1, std::min(nchunk, ceil_div(2 * nsm, ctiles)));
@@ -541,15 +631,13 @@ int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, in
   a1.ncols = ncols;
   a1.nrm = nrm;
   a1.vb1 = vb1;
-  a1.s = s;
   a1.chunks_per_split = cps;
   a1.Wp = Wp;
   a1.npad = npad;
   a1.st = st;
-  k_oz_gemm1<<<dim3(ctiles, nsplit), OZ_TPB, oz_gemm_smem(s), st_>>>(a1);
+  k_oz_gemm1<S><<<dim3(ctiles, nsplit), OZ_TPB, oz_gemm1_smem(S), st_>>>(a1);
   const int wtiles = ceil_div(ncols - 1, 64);
-  k_oz_w2<<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nsplit, npad, T, ldt, ncols, s, st, wb2,
-                                                                wexp);
+  k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nsplit, npad, T, ldt, ncols, st, wb2, wexp);
   OzG2Args a2;
   a2.W0 = W0;
   a2.lda = lda;
@@ -558,11 +646,27 @@ int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, in
   a2.va2 = va2;
   a2.wb2 = wb2;
   a2.wexp = wexp;
-  a2.s = s;
   a2.st = st;
-  k_oz_gemm2<<<dim3(wtiles, ceil_div(mloc, 128)), OZ_TPB, oz_gemm_smem(s), st_>>>(a2);
-  if (launches) *launches += 4;
+  k_oz_gemm2<S><<<dim3(wtiles, ceil_div(mloc, 128)), OZ_TPB, oz_gemm2_smem(S), st_>>>(a2);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+// Whole mixed-precision trailing update of one DM block.  Buffers: va2/vb1
+// (V digits), wb2 (W2 digits), wexp (n ints), Wp (nsplit x npad x 64 FP64).
+int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
+                       const double* T, int ldt, int s, int nsm, BlockState* st, unsigned char* va2,
+                       unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp, int* launches) {
+  if (ncols <= 1 || mloc <= 0) return 0;
+  int r = 1;
+  switch (s) {
+    case 4: r = oz_run<4>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 5: r = oz_run<5>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 6: r = oz_run<6>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 7: r = oz_run<7>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    default: return 1;
+  }
+  if (launches) *launches += 4;
+  return r;
 }
 
 // Workspace bytes of the mixed trailing update for an m x n problem.
