@@ -52,6 +52,7 @@ WORKLOADS = {
     "batched2000": (0, 0, "2000 uneven U diag(s) V^T, n in [32, 512], m = n r, r in [1, 4]"),
 }
 BATCH_COUNT, BATCH_NB = 2000, 32
+BATCH_GENERATOR = None
 BATCH_CPU_SAMPLE = 400
 FP64_PEAK_TFLOPS = 1.25  # nominal dense FP64 of GB300 (no measured FP64 peak)
 NB, DELTA, TAU_ = 64, 0.9, 0.15
@@ -316,11 +317,17 @@ def run_ours(args):
         peaks, peak_kind = load_peaks()
         phase = {"select": sti.ms_select, "panel": sti.ms_panel, "tfactor": sti.ms_tfactor,
                  "trail": sti.ms_trail, "norm": sti.ms_norm}
+        pcy = (C.c_ulonglong * 8)()
+        L.qrdm_panel_phase_cycles(pcy, 8)
+        if pcy[7]:
+            pnames = ["cluster_sync", "cluster_sum", "grid_barrier", "cross_sum", "scalars",
+                      "apply", "partials"]
+            phase["panel_cta0_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames)}
         nblk = int(sti.nblocks)
         if prec == 0:
             # FP64 FMA GEMMs: no measured FP64 peak exists for this machine;
             # GB300's nominal dense FP64 rate is used
-            achieved = sti.trail_flops / (sti.ms_trail / 1e3) / 1e12
+            achieved = sti.trail_flops / (sti.ms_trail / 1e3) / 1e12 if sti.ms_trail > 0 else 0.0
             roof = {"bound": "tensor", "kernel": "trailing update (k_trail_w_partial + "
                     "k_trail_w_reduce + k_trail_update), FP64 FMA", "achieved": achieved,
                     "peak": 1.25, "peak_kind": "nominal FP64 (no measured FP64 peak)",
@@ -333,7 +340,7 @@ def run_ours(args):
             s_dig = int(default_options().slices) or 7
             prods = s_dig * (s_dig + 1) // 2
             tflop = sti.trail_flops * prods
-            achieved = tflop / (sti.ms_trail / 1e3) / 1e12
+            achieved = tflop / (sti.ms_trail / 1e3) / 1e12 if sti.ms_trail > 0 else 0.0
             peak = peaks.get("bf16_tflops_sustained")
             roof = {"bound": "tensor", "kernel": "Ozaki trailing update (k_oz_slice_v, "
                     "k_oz_gemm1, k_oz_w2, k_oz_gemm2), BF16 tcgen05", "achieved": achieved,
@@ -342,7 +349,8 @@ def run_ours(args):
                     "traffic": load_traffic("trail_ozaki"),
                     "per_launch_basis": f"{prods} BF16 digit products x 4 m' n' k flops per DM "
                                         f"block, {nblk} blocks",
-                    "fp64_equivalent_tflops": sti.trail_flops / (sti.ms_trail / 1e3) / 1e12}
+                    "fp64_equivalent_tflops": (sti.trail_flops / (sti.ms_trail / 1e3) / 1e12
+                                               if sti.ms_trail > 0 else 0.0)}
         # e2e through the host C ABI with pinned host buffers
         a_host = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
         a_host.copy_(pristine)
@@ -446,8 +454,18 @@ def batched_setup(seed=4, count=None):
     ms, ns = batched_shapes(count or BATCH_COUNT, seed=seed)
     shapes = [(int(m), int(n)) for m, n in zip(ms, ns)]
     b = BatchedDMQR(shapes)
-    for i, (m, n) in enumerate(shapes):
-        b.a[b.a_off[i]:b.a_off[i + 1]] = batched_problem_device(i, m, n, seed)
+    global BATCH_GENERATOR
+    try:
+        for i, (m, n) in enumerate(shapes):
+            b.a[b.a_off[i]:b.a_off[i + 1]] = batched_problem_device(i, m, n, seed)
+        BATCH_GENERATOR = "torch (GPU QR of seeded Gaussians)"
+    except RuntimeError:
+        # torch's GPU linear algebra can be unavailable (e.g. under a
+        # profiler): same distribution from the host generator
+        from qrdm_gb300.workloads import batched_matrix
+
+        b.load([batched_matrix(i, m, n, seed) for i, (m, n) in enumerate(shapes)])
+        BATCH_GENERATOR = "numpy (host QR of seeded Gaussians)"
     torch.cuda.synchronize()
     return b, shapes
 
@@ -560,7 +578,10 @@ def run_batched(args):
         phases = {nm: float(cyc[k]) / busy for k, nm in enumerate(names)}
         nsm = torch.cuda.get_device_properties(local).multi_processor_count
         phases["longest_over_mean_cta"] = float(cyc[8]) / (busy / nsm)
-        be, orth = batched_errors(b, pristine)
+        try:
+            be, orth = batched_errors(b, pristine)
+        except RuntimeError:  # torch's GPU linear algebra unavailable
+            be, orth = np.full(1, np.nan), np.full(1, np.nan)
         achieved = F / (kms / 1e3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch)",
                 "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
@@ -601,7 +622,7 @@ def run_batched(args):
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic",
                "config": {"workload": "batched2000", "count": count, "nb": BATCH_NB,
-                          "delta": DELTA, "tau_": TAU_, "flops": F,
+                          "delta": DELTA, "tau_": TAU_, "flops": F, "generator": BATCH_GENERATOR,
                           "bytes": 8 * pristine.numel(),
                           "parallelism": f"replicas{world}",
                           "l2": "inputs (3.3 GB) larger than L2; no flush needed"},

@@ -131,6 +131,13 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
  * lifetime.  Instrumentation only (no counterpart in the reference). */
 int qrdm_batched_phase_cycles(unsigned long long* out, int nout);
 
+/* Clustered-panel phase cycles of CTA 0 summed over the panels of the last
+ * DM-QR call made with stats.timing = 1: out[0..7] = cluster barrier,
+ * cluster reduction, grid barrier, cross-cluster sum, reflector scalars,
+ * reflector application, next-column partials, kernel lifetime.
+ * Instrumentation only (no counterpart in the reference). */
+int qrdm_panel_phase_cycles(unsigned long long* out, int nout);
+
 /* ------------------------------------------------------------------ QP3 */
 /* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot
  * per column by largest partial norm, first index on ties; jpvt[j] != 0

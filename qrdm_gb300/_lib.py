@@ -46,6 +46,7 @@ SIGNATURES = {
     "dgeqrdm_batched_dev": (C.c_int, [C.c_int, _pi, _pi, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.c_void_p, C.c_void_p, _pd, C.c_int, C.c_int]),
     "qrdm_batched_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
+    "qrdm_panel_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     "dgeqp3": (C.c_int, [C.c_int, C.c_int, C.c_int, _pd, C.c_int, _pi, _pd]),
     "dgeqp3_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                              C.c_void_p]),

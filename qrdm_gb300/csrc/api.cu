@@ -249,7 +249,7 @@ static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t 
   for (int attempt = 0; attempt < 3 && ncl > 0; ++attempt) {
     const int G = ncl * kPanelClusterSize;
     const int R = ceil_div(mloc, G);
-    const size_t smem = (size_t)R * kmax * sizeof(double);
+    const size_t smem = (size_t)(R | 1) * kmax * sizeof(double);  // odd slab stride
     if (smem + 8192 > c.smem_optin) break;
     const int cap = panel_cluster_capacity(smem);
     if (cap <= 0) break;
@@ -309,6 +309,10 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   CK(c.perm.ensure(ws.perm));
   CK(c.st.ensure(ws.st));
   CK(c.pan_part.ensure(ws.pan_part));
+  if (timing) {
+    CK(c.pan_prof.ensure(sizeof(unsigned long long) * 8));
+    CK(cudaMemsetAsync(c.pan_prof.p, 0, sizeof(unsigned long long) * 8, s));
+  }
   CK(c.pan_row.ensure(ws.pan_row));
   CK(c.pan_bar.ensure(ws.pan_bar));
   CK(c.vtv_part.ensure(ws.vtv_part));
@@ -439,6 +443,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       pa.vtv_part = c.vtv_part.as<double>();
       pa.rows_per_cta = 1;
       pa.allow_exit = 1;
+      pa.prof = timing ? c.pan_prof.as<unsigned long long>() : nullptr;
       RET(launch_panel(c, pa, mloc, kmax, s, &G));
     }
     PH(2);
@@ -630,6 +635,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
     pa.vtv_part = c.vtv_part.as<double>();
     pa.rows_per_cta = 1;
     pa.allow_exit = 0;
+    pa.prof = nullptr;
     RET(launch_panel(c, pa, mloc, kb, s, &G));
     int npair = kb * (kb - 1) / 2;
     k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
@@ -1160,6 +1166,21 @@ int qrdm_batched_phase_cycles(unsigned long long* out, int nout) {
   return 0;
 }
 
+int qrdm_panel_phase_cycles(unsigned long long* out, int nout) {
+  if (!out || nout <= 0) return -1;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  for (int k = 0; k < nout; ++k) out[k] = 0;
+  if (!c->pan_prof.p) return 0;
+  unsigned long long h[8];
+  CK(cudaMemcpyAsync(h, c->pan_prof.p, sizeof h, cudaMemcpyDeviceToHost, c->stream()));
+  CK(cudaStreamSynchronize(c->stream()));
+  for (int k = 0; k < nout && k < 8; ++k) out[k] = h[k];
+  return 0;
+}
+
 int qrdm_set_stream(void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx* c = nullptr;
@@ -1180,7 +1201,7 @@ int qrdm_release_workspace(void) {
   Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
                  &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
                  &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst,
-                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws, &c.b_prof};
+                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws, &c.b_prof, &c.pan_prof};
   if (c.b_graph) {
     cudaGraphExecDestroy(c.b_graph);
     c.b_graph = nullptr;

@@ -53,6 +53,7 @@ struct Ctx {
   Buf qF, qg, qpart, qst;
   Buf oz_va2, oz_vb1, oz_wb2, oz_wexp, oz_wp;  // mixed-precision trailing update
   Buf b_meta, b_ws, b_prof;                     // batched DM-QR
+  Buf pan_prof;                                 // clustered panel phase cycles (timing runs)
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch
   unsigned long long b_key = 0;
   BlockState* h_st = nullptr;              // pinned host copy of the block record

@@ -29,6 +29,7 @@ struct PanelArgs {
   double* vtv_part;   // [G][NB_MAX][NB_MAX]
   int rows_per_cta;
   int allow_exit;     // 1: DM early exit (dgeqr2_mia); 0: plain dgeqr2
+  unsigned long long* prof;  // clustered panel: CTA 0's per-phase cycles [8] (added to), or null
 };
 
 struct TrailArgs {

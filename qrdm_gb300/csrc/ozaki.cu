@@ -87,6 +87,7 @@ __device__ __forceinline__ unsigned short bf16_bits(int d) {
 }
 // exact FP32 integer (|x| < 2^31) -> int32
 __device__ __forceinline__ int f32_to_int(float x) { return __float2int_rn(x); }
+
 // 2^e as a double (normal range), built from its bit pattern
 __device__ __forceinline__ double pow2d(int e) {
   e = e < -1022 ? -1022 : (e > 1023 ? 1023 : e);
@@ -414,7 +415,7 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
 }
 
 // ------------------------------------------- W2 = T^T W and its digits
-// One CTA per 16 C-columns (a quarter of a 64-row GEMM2 B tile): sum the
+// One CTA per 16 C-columns (half of a 32-row GEMM2 B tile): sum the
 // split partials (fixed order, eight loads in flight), apply T^T, then slice
 // W2 per column (scale 2^(E+1) of the column max) into the GEMM2 B tiles
 // wb2[tile][q] (N = C column, K = reflector column).
@@ -483,7 +484,7 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
   }
   __syncthreads();
   // digits: thread -> (column cc, reflector pair ap); tile rows = columns
-  const int tile = cbase / 64, row0 = cbase % 64;
+  const int tile = cbase / 32, row0 = cbase % 32;
   for (int e = threadIdx.x; e < OZ_W2_COLS * 32; e += blockDim.x) {
     const int cc = e / 32, ap = e % 32;
     const int sh = 8 * S - scale_exp_of(smax[cc]);
@@ -493,14 +494,22 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
     const uint32_t off = tc::sw128_offset(row0 + cc, 2 * ap);
 #pragma unroll
     for (int q = 0; q < S; ++q)
-      *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * S + q) * 8192 + off) = pack2_bf16(d0[q], d1[q]);
+      *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * S + q) * 4096 + off) = pack2_bf16(d0[q], d1[q]);
   }
 }
 
 // ------------------------------------------------------------- GEMM 2
-// C(r, c) -= V(r, :) W2(:, c) for a 128-row x 64-column tile of C
-// (C columns start at window column st->fjb).  Both digit operands arrive by
-// bulk copies; the tile's C entries are loaded while the tensor core works.
+// C(r, c) -= V(r, :) W2(:, c), persistent and pipelined.  Work items are
+// 128-row x 32-column tiles of C in band-major order; each CTA takes a
+// contiguous range.  Warp 8 (one lane) is the producer and MMA issuer: it
+// keeps the V digits of the current 128-row band resident (one bulk copy per
+// band), streams the W2 digits of each 32-column tile through a ring of
+// NST2 stages (bulk copies), and accumulates each tile's S levels into one
+// of two TMEM buffers.  Warps 0..7 are the epilogue: each owns 32 rows
+// (its TMEM lane quadrant) x 16 columns of a tile, loads its C entries
+// before the tile's MMAs finish, recombines the levels and writes C back,
+// then frees the TMEM buffer, so the next tile's MMAs overlap this tile's
+// epilogue.
 struct OzG2Args {
   double* W0;
   long long lda;
@@ -511,89 +520,161 @@ struct OzG2Args {
   BlockState* st;
 };
 
+constexpr int OZ_G2_THREADS = 288;  // 8 epilogue warps + 1 producer warp
+constexpr int NST2 = 3;              // W2 digit stages
+
 template <int S>
-__global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm2(OzG2Args g) {
+__global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  unsigned char* adig = base;              // S x 16 KB
-  unsigned char* bdig = base + S * 16384;  // S x 8 KB
-  __shared__ uint64_t bar, lbar;
+  unsigned char* adig = base;              // S x 16 KB: V digits of one band
+  unsigned char* bring = base + S * 16384;  // NST2 x S x 4 KB: W2 digits of a tile
+  constexpr uint32_t ABYTES = S * 16384, BBYTES = S * 4096;
+  __shared__ uint64_t aload, full[NST2], empty[NST2], tfull[2], tempty[2];
   __shared__ uint32_t s_tmem;
-  __shared__ int s_ok;
   const int fjb = g.st->fjb;
   const int k = g.st->fjb_cmp;
-  const int ct = blockIdx.x, rt = blockIdx.y;
-  const int cw0 = ct * 64;  // first C column relative to fjb
-  if (fjb + cw0 >= g.ncols || rt * 128 >= g.mloc || k <= 0) return;
-  const int tid = threadIdx.x;
+  const int n2 = g.ncols - fjb;
+  if (n2 <= 0 || k <= 0) return;
+  const int ntile = ceil_div(n2, 32), nband = ceil_div(g.mloc, 128);
+  const int nitems = ntile * nband;
+  const int per = ceil_div(nitems, (int)gridDim.x);
+  const int first = blockIdx.x * per;
+  const int nmine = max(0, min(nitems, first + per) - first);
+  if (nmine == 0) return;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    tc::mbar_init(&bar, 1);
-    tc::mbar_init(&lbar, 1);
+    tc::mbar_init(&aload, 1);
+    for (int i = 0; i < NST2; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&tfull[i], 1);
+      tc::mbar_init(&tempty[i], 8);
+    }
     tc::fence_mbar_init();
-    tc::mbar_arrive_expect_tx(&lbar, S * (16384 + 8192));
-    tc::bulk_g2s(adig, g.va2 + (size_t)rt * S * 16384, S * 16384, &lbar);
-    tc::bulk_g2s(bdig, g.wb2 + (size_t)ct * S * 8192, S * 8192, &lbar);
   }
-  if (tid < 32) tc::tmem_alloc(&s_tmem, 512);
+  if (w == 0) tc::tmem_alloc(&s_tmem, 512);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
-  if (tid == 0) {
-    const bool loaded = tc::mbar_wait(&lbar, 0);
-    if (loaded) oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig), 0, 4, true);
-    tc::mma_commit(&bar);
-    s_ok = loaded ? 1 : 0;
-  }
-  const int w = tid >> 5, lane = tid & 31;
-  const int rr = 32 * (w & 3) + lane;
-  const int half = tid >> 7;
-  const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
-  const int r = rt * 128 + rr;
-  // fetch this thread's 32 entries of C while the tensor core works
-  double cv[32];
+  bool fail = false;
+  if (w == 8) {
+    if (lane == 0) {
+      auto produce = [&](int kk) {
+        const int it = first + kk, t = it % ntile, stg = kk % NST2;
+        tc::mbar_arrive_expect_tx(&full[stg], BBYTES);
+        tc::bulk_g2s(bring + stg * BBYTES, g.wb2 + (size_t)t * BBYTES, BBYTES, &full[stg]);
+      };
+      const int pre = min(NST2, nmine);
+      for (int kk = 0; kk < pre; ++kk) produce(kk);
+      int band_loaded = -1;
+      uint32_t aph = 0;
+      for (int kk = 0; kk < nmine; ++kk) {
+        const int it = first + kk, band = it / ntile, stg = kk % NST2, b = kk & 1;
+        if (band != band_loaded) {
+          // every MMA so far has completed before the band's V digits change
+          if (kk > 0 && !tc::mbar_wait(&tfull[(kk - 1) & 1], (uint32_t)(((kk - 1) >> 1) & 1))) fail = true;
+          tc::mbar_arrive_expect_tx(&aload, ABYTES);
+          tc::bulk_g2s(adig, g.va2 + (size_t)band * ABYTES, ABYTES, &aload);
+          if (!tc::mbar_wait(&aload, aph)) fail = true;
+          aph ^= 1u;
+          band_loaded = band;
+        }
+        if (!tc::mbar_wait(&full[stg], (uint32_t)((kk / NST2) & 1))) fail = true;
+        if (kk >= 2 && !tc::mbar_wait(&tempty[b], (uint32_t)(((kk - 2) >> 1) & 1))) fail = true;
+        tc::fence_after_sync();
+        if (!fail) {
+          const uint32_t acc = tmem + (uint32_t)(b * 256);
+          const uint32_t a0 = tc::smem_u32(adig), b0 = tc::smem_u32(bring + stg * BBYTES);
 #pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    const int c = fjb + cw0 + 32 * half + i;
-    cv[i] = (r < g.mloc && c < g.ncols) ? g.W0[(size_t)c * g.lda + r] : 0.0;
-  }
-  bool ok = tc::mbar_wait(&bar, 0);
-  __syncthreads();
-  ok = ok && s_ok;
-  if (!ok && tid == 0) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
-  tc::fence_after_sync();
-  if (ok) {
+          for (int p = 1; p <= S; ++p) {
+            const uint32_t idesc = tc::idesc_bf16_f32(128, 32 * (S + 1 - p));
 #pragma unroll
-    for (int g8 = 0; g8 < 4; ++g8) {
-      long long hi[8], mid[8];
-      oz_levels8<S>(taddr, 32 * half + 8 * g8, hi, mid);
-      if (r < g.mloc) {
+            for (int q4 = 0; q4 < 4; ++q4)
+              tc::mma_bf16(acc + (uint32_t)((p - 1) * 32), tc::desc_sw128(a0 + (uint32_t)(p - 1) * 16384u + q4 * 32),
+                           tc::desc_sw128(b0 + q4 * 32), idesc, (p == 1 && q4 == 0) ? 0u : 1u);
+          }
+        }
+        tc::mma_commit(&empty[stg]);
+        tc::mma_commit(&tfull[b]);
+        // refill the stage the previous tile used (its MMAs finish first)
+        if (kk >= 1 && kk - 1 + NST2 < nmine) {
+          const int ps = (kk - 1) % NST2;
+          if (!tc::mbar_wait(&empty[ps], (uint32_t)(((kk - 1) / NST2) & 1))) fail = true;
+          produce(kk - 1 + NST2);
+        }
+      }
+      // the last stages' commits and copies have landed before exit
+      for (int kk = max(0, nmine - NST2); kk < nmine; ++kk)
+        tc::mbar_wait(&empty[kk % NST2], (uint32_t)((kk / NST2) & 1));
+    }
+  } else {
+    // epilogue: rows 32 (w & 3) + lane of the band, columns 16 (w >> 2) + j
+    const int quad = w & 3, ch = w >> 2;
+    const uint32_t tl = tmem + ((uint32_t)(32 * quad) << 16);
+    for (int kk = 0; kk < nmine; ++kk) {
+      const int it = first + kk, band = it / ntile, t = it % ntile, b = kk & 1;
+      const int r = band * 128 + 32 * quad + lane;
+      const int cw0 = t * 32 + 16 * ch;  // C column relative to fjb
+      double cv[16];
 #pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          const int cw = cw0 + 32 * half + 8 * g8 + i;
-          const int c = fjb + cw;
+      for (int j = 0; j < 16; ++j) {
+        const int c = fjb + cw0 + j;
+        cv[j] = (r < g.mloc && c < g.ncols) ? g.W0[(size_t)c * g.lda + r] : 0.0;
+      }
+      if (!tc::mbar_wait(&tfull[b], (uint32_t)((kk >> 1) & 1))) fail = true;
+      tc::fence_after_sync();
+      long long hi[16], mid[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        hi[j] = 0;
+        mid[j] = 0;
+      }
+#pragma unroll
+      for (int L = 2; L <= S + 1; ++L) {
+        float v[16];
+        tc::tmem_ld16(tl + (uint32_t)(b * 256 + (L - 2) * 32 + 16 * ch), v);
+        tc::tmem_wait_ld();
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const long long x = (long long)f32_to_int(v[j]);
+          if (L <= 5) hi[j] += x << (8 * (5 - L));
+          else mid[j] += x << (8 * (S + 1 - L));
+        }
+      }
+      tc::fence_before_sync();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&tempty[b]);
+      if (!fail && r < g.mloc) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int cw = cw0 + j, c = fjb + cw;
           if (c < g.ncols) {
             const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
-            // U = 2^e (hi 256^-5 + mid 256^-(S+1)).  hi < 2^45 and
-            // mid < 2^40, so hi 2^17 + mid 2^(57-8S) fits in 62 bits and keeps
-            // ~2^-62 of U: one conversion, one FP64 subtraction.
-            constexpr int msh = 8 * (S + 1) - 40 - 17;  // weight of mid relative to hi 2^17
-            const long long comb = (hi[i] << 17) + (msh >= 0 ? (mid[i] >> msh) : (mid[i] << -msh));
-            const double u = (double)comb * pow2d(e - 40 - 17);
-            g.W0[(size_t)c * g.lda + r] = cv[8 * g8 + i] - u;
+            // U = 2^e (hi 256^-5 + mid 256^-(S+1)).  hi < 2^45 and mid <
+            // 2^40, so hi 2^17 + mid 2^(57-8S) fits in 62 bits and keeps
+            // ~2^-62 of U; the power-of-two scale is exact, so one FMA rounds
+            // once, as a multiply and a subtraction would.
+            constexpr int msh = 8 * (S + 1) - 40 - 17;
+            const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
+            g.W0[(size_t)c * g.lda + r] = fma(-(double)comb, pow2d(e - 40 - 17), cv[j]);
           }
         }
       }
     }
   }
+  if (fail) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
   tc::fence_before_sync();
   __syncthreads();
-  if (tid < 32) tc::tmem_dealloc(tmem, 512);
+  if (w == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // ------------------------------------------------------------ launchers
 static size_t oz_gemm1_smem(int s) { return (size_t)s * (16384 + 2 * 8192) + 1024; }
-static size_t oz_gemm2_smem(int s) { return (size_t)s * (16384 + 8192) + 1024; }
+static size_t oz_gemm2_smem(int s) { return (size_t)s * (16384 + NST2 * 4096) + 1024; }
 size_t oz_gemm_smem(int s) { return oz_gemm1_smem(s); }
 
 template <int S>
@@ -636,7 +717,6 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
   a1.npad = npad;
   a1.st = st;
   k_oz_gemm1<S><<<dim3(ctiles, nsplit), OZ_TPB, oz_gemm1_smem(S), st_>>>(a1);
-  const int wtiles = ceil_div(ncols - 1, 64);
   k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nsplit, npad, T, ldt, ncols, st, wb2, wexp);
   OzG2Args a2;
   a2.W0 = W0;
@@ -647,7 +727,8 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
   a2.wb2 = wb2;
   a2.wexp = wexp;
   a2.st = st;
-  k_oz_gemm2<S><<<dim3(wtiles, ceil_div(mloc, 128)), OZ_TPB, oz_gemm2_smem(S), st_>>>(a2);
+  const int items = ceil_div(ncols - 1, 32) * ceil_div(mloc, 128);
+  k_oz_gemm2<S><<<std::max(1, std::min(nsm, items)), OZ_G2_THREADS, oz_gemm2_smem(S), st_>>>(a2);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
@@ -674,7 +755,7 @@ void oz_workspace(int m, int n, int s, int nsm, size_t* va2, size_t* vb1, size_t
                   size_t* wp) {
   *va2 = (size_t)ceil_div(m, 256) * 2 * s * 16384;
   *vb1 = (size_t)ceil_div(m, 256) * 4 * s * 8192;
-  *wb2 = (size_t)ceil_div(n, 64) * s * 8192;
+  *wb2 = (size_t)ceil_div(n, 32) * s * 4096;
   *wexp = sizeof(int) * (size_t)n;
   const int ctiles = ceil_div(n, 128);
   const int nchunk = ceil_div(m, 256);

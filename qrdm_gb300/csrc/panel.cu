@@ -217,6 +217,31 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
   if (g == 0 && threadIdx.x == 0) p.st->fjb_cmp = kc;
 }
 
+// Partials for the clustered panel: one thread per slot, each summing its
+// dot product over this CTA's rows in two interleaved chains.  On GB300 an
+// FP64 warp instruction costs the SM's FP64 pipe the same whatever its
+// active lanes, so slots-across-lanes (no shuffle reductions) issues about a
+// fifth of the FP64 instructions of rows-across-lanes.  Columns are LS
+// (odd) doubles apart, so the 32 lanes' loads hit distinct banks.
+__device__ __forceinline__ void panel_partials_slots(const double* __restrict__ S, int LS, int nr, int grow0,
+                                                    int i, int fjb, double* __restrict__ out) {
+  const int nslot = fjb - i;
+  int rr0 = i + 1 - grow0;  // first local row strictly below the diagonal
+  if (rr0 < 0) rr0 = 0;
+  const double* x = S + (size_t)i * LS;
+  for (int sl = threadIdx.x; sl < nslot; sl += blockDim.x) {
+    const double* y = S + (size_t)(i + sl) * LS;
+    double a0 = 0.0, a1 = 0.0;
+    int rr = rr0;
+    for (; rr + 1 < nr; rr += 2) {
+      a0 = fma(x[rr], y[rr], a0);
+      a1 = fma(x[rr + 1], y[rr + 1], a1);
+    }
+    if (rr < nr) a0 = fma(x[rr], y[rr], a0);
+    out[sl] = a0 + a1;
+  }
+}
+
 // ------------------------------------------------ clustered panel (K-panel)
 // Same arithmetic as k_panel, launched as clusters of kPanelCluster CTAs:
 // per column, each CTA's partial slots are summed by its cluster leader
@@ -229,15 +254,17 @@ constexpr int kPanelCluster = 8;
 
 __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* S = reinterpret_cast<double*>(smem_raw);  // [fjb][R]
+  double* S = reinterpret_cast<double*>(smem_raw);  // [fjb][LS]
   __shared__ PanelSmem sm;
   __shared__ double s_part[2][QRDM_NB_MAX + 1];
+  __shared__ double s_row[QRDM_NB_MAX];
   cg::cluster_group cl = cg::this_cluster();
   // cluster shape as launched (the DSMEM reads below only address ranks
   // that exist, whatever cluster size the kernel actually runs with)
   const unsigned crank = cl.block_rank();
   const int csize = (int)cl.num_blocks();
   const int G = gridDim.x, g = blockIdx.x, R = p.rows_per_cta;
+  const int LS = R | 1;  // column stride of the slab (odd: conflict-free per-slot loads)
   const int ncl = G / csize, cid = g / csize;
   const int fjb = p.st->fjb;
   const int grow0 = g * R;
@@ -255,12 +282,12 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
   __syncthreads();
   for (int e = tid; e < fjb * nr; e += blockDim.x) {
     int c = e / nr, rr = e % nr;
-    S[(size_t)c * R + rr] = W0[(size_t)c * lda + grow0 + rr] * sm.sc[c];
+    S[(size_t)c * LS + rr] = W0[(size_t)c * lda + grow0 + rr] * sm.sc[c];
   }
   __syncthreads();
-  panel_partials(S, R, nr, grow0, 0, fjb, s_part[0]);
+  panel_partials_slots(S, LS, nr, grow0, 0, fjb, s_part[0]);
   if (grow0 <= 0 && 0 < grow0 + nr)
-    for (int c = tid; c < fjb; c += blockDim.x) p.rowbuf[c] = S[(size_t)c * R + (0 - grow0)];
+    for (int c = tid; c < fjb; c += blockDim.x) p.rowbuf[c] = S[(size_t)c * LS + (0 - grow0)];
 
   // Every CTA executes exactly fjb + 1 cluster barriers whatever happens
   // (early exit, barrier timeout), so no CTA can wait at a cluster barrier
@@ -269,23 +296,46 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
   int done = fjb;
   bool ok = true;
   bool active = true;
+  // phase clock of CTA 0 (instrumentation; p.prof null in normal runs)
+  const bool prof = p.prof != nullptr && g == 0 && tid == 0;
+  unsigned long long pc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  long long tlast = clock64();
+  const long long tstart = tlast;
+#define PPH(k)                                   \
+  do {                                           \
+    if (prof) {                                  \
+      const long long now_ = clock64();          \
+      pc[(k)] += (unsigned long long)(now_ - tlast); \
+      tlast = now_;                              \
+    }                                            \
+  } while (0)
   for (int i = 0; i < fjb; ++i) {
     const int buf = i & 1;
     const int nslot = fjb - i;
     double* part = p.part + (size_t)buf * ncl * stride;
     const double* rowb = p.rowbuf + (size_t)buf * (QRDM_NB_MAX + 2);
+    PPH(6);
     cl.sync();
+    PPH(0);
     if (!active) continue;
-    // 1. cluster: leader sums the member partials (DSMEM, fixed order)
+    // 1. cluster: leader sums the member partials (DSMEM, fixed order; all
+    //    remote loads issued before the sum)
     if (crank == 0) {
       for (int sl = tid; sl < nslot; sl += blockDim.x) {
+        double v[kPanelCluster];
+#pragma unroll
+        for (int r = 0; r < kPanelCluster; ++r)
+          v[r] = r < csize ? cl.map_shared_rank(&s_part[buf][0], r)[sl] : 0.0;
         double acc = 0.0;
-        for (int r = 0; r < csize; ++r) acc += cl.map_shared_rank(&s_part[buf][0], r)[sl];
+#pragma unroll
+        for (int r = 0; r < kPanelCluster; ++r)
+          if (r < csize) acc += v[r];
         part[(size_t)cid * stride + sl] = acc;
       }
     }
     // 2. grid: leaders arrive, everyone waits (bounded) for all leaders
     __syncthreads();
+    PPH(1);
     if (tid == 0) {
       if (crank == 0) {
         __threadfence();
@@ -304,26 +354,42 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
       __threadfence();
     }
     __syncthreads();
+    PPH(2);
     if (sm.exit_flag == 2) {
       ok = false;
       active = false;
       continue;
     }
-    // 3. fixed-order sum of the cluster totals: 4 threads per slot
+    // 3. fixed-order sum of the cluster totals: 4 threads per slot, every
+    //    load in flight before the adds; row i of the panel (published by
+    //    its owner) fetched alongside
+    for (int c = i + tid; c < fjb; c += blockDim.x) s_row[c] = __ldcg(rowb + c);
     for (int base = 0; base < nslot; base += 64) {
       const int sl = base + (tid >> 2), q0 = tid & 3;
       double acc = 0.0;
-      if (sl < nslot)
-        for (int q = q0; q < ncl; q += 4) acc += __ldcg(part + (size_t)q * stride + sl);
+      if (sl < nslot) {
+        for (int qb = q0; qb < ncl; qb += 32) {
+          double v[8];
+#pragma unroll
+          for (int u = 0; u < 8; ++u) {
+            const int q = qb + 4 * u;
+            v[u] = q < ncl ? __ldcg(part + (size_t)q * stride + sl) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < 8; ++u)
+            if (qb + 4 * u < ncl) acc += v[u];
+        }
+      }
       acc += __shfl_xor_sync(0xffffffffu, acc, 1);
       acc += __shfl_xor_sync(0xffffffffu, acc, 2);
       if (sl < nslot && q0 == 0) sm.red[sl] = acc;
     }
     __syncthreads();
+    PPH(3);
     // 4. dlarfg scalars (thread 0), then w_c in parallel
     if (tid == 0) {
       const double sci = sm.sc[i];
-      const double alpha = __ldcg(rowb + i);
+      const double alpha = s_row[i];
       const int order = p.mloc - i;
       sm.tau_zero = 1;
       sm.tau = 0.0;
@@ -354,45 +420,52 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
       continue;
     }
     for (int c = i + 1 + tid; c < fjb; c += blockDim.x) {
-      const double w = __ldcg(rowb + c) + sm.scal * sm.red[c - i];
+      const double w = s_row[c] + sm.scal * sm.red[c - i];
       sm.tw[c] = sm.tau * w;
     }
     __syncthreads();
+    PPH(4);
     // 5. apply H(i) to this CTA's rows, then the partials of column i+1
     if (!sm.tau_zero) {
       const double scal = sm.scal;
       const int ncol_r = fjb - i - 1;
       int rr0 = i + 1 - grow0;
       if (rr0 < 0) rr0 = 0;
-      double* x = S + (size_t)i * R;
+      double* x = S + (size_t)i * LS;
       for (int rr = rr0 + tid; rr < nr; rr += blockDim.x) x[rr] *= scal;
       __syncthreads();
       for (int e = tid; e < ncol_r * nr; e += blockDim.x) {
         int cc = e / nr, rr = e % nr;
         int c = i + 1 + cc;
         int grow = grow0 + rr;
-        if (grow > i) S[(size_t)c * R + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * R + rr]);
-        else if (grow == i) S[(size_t)c * R + rr] -= sm.tw[c];
+        if (grow > i) S[(size_t)c * LS + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * LS + rr]);
+        else if (grow == i) S[(size_t)c * LS + rr] -= sm.tw[c];
       }
       if (grow0 <= i && i < grow0 + nr && tid == 0) x[i - grow0] = sm.beta;
     }
     __syncthreads();
+    PPH(5);
     if (i + 1 < fjb) {
-      panel_partials(S, R, nr, grow0, i + 1, fjb, s_part[buf ^ 1]);
+      panel_partials_slots(S, LS, nr, grow0, i + 1, fjb, s_part[buf ^ 1]);
       if (grow0 <= i + 1 && i + 1 < grow0 + nr) {
         double* rb = p.rowbuf + (size_t)(buf ^ 1) * (QRDM_NB_MAX + 2);
-        for (int c = i + 1 + tid; c < fjb; c += blockDim.x) rb[c] = S[(size_t)c * R + (i + 1 - grow0)];
+        for (int c = i + 1 + tid; c < fjb; c += blockDim.x) rb[c] = S[(size_t)c * LS + (i + 1 - grow0)];
       }
     }
   }
   // keep every CTA's shared memory alive until the leader's last DSMEM read
   cl.sync();
+  if (prof) {
+    pc[7] = (unsigned long long)(clock64() - tstart);
+    for (int k = 0; k < 8; ++k) atomicAdd(p.prof + k, pc[k]);
+  }
+#undef PPH
   if (!ok) return;
   const int kc = done;
   for (int e = tid; e < fjb * nr; e += blockDim.x) {
     int c = e / nr, rr = e % nr;
     int grow = grow0 + rr;
-    double v = S[(size_t)c * R + rr];
+    double v = S[(size_t)c * LS + rr];
     if (!(c < kc && grow > c)) v = v / sm.sc[c];
     W0[(size_t)c * lda + grow] = v;
   }
@@ -403,8 +476,8 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     while (b * (b - 1) / 2 > t) --b;
     while ((b + 1) * b / 2 <= t) ++b;
     int a = t - b * (b - 1) / 2;
-    const double* va = S + (size_t)a * R;
-    const double* vb = S + (size_t)b * R;
+    const double* va = S + (size_t)a * LS;
+    const double* vb = S + (size_t)b * LS;
     double acc = 0.0;
     int rstart = b - grow0;
     if (rstart < 0) rstart = 0;
