@@ -203,13 +203,15 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 // over the 256-row chunks [chunk_begin, chunk_end) of the window.
 // Wp[split][c][a] (FP64).  C columns start at window column st->fjb.
 //
-// Pipeline per 64-row block: the C digits (A operand, converted from FP64 by
-// all threads) are written half a block (32 rows = K16 steps 2h, 2h+1) at a
-// time, so converting one half overlaps the tensor core's work on the other;
-// each half's MMAs commit to their own mbarrier, which frees that half.  The
-// V digits (B operand) of the next block arrive by one bulk copy into the
-// second of two buffers.  C loads for the next half are issued before the
-// current half's digits are stored.
+// Warp-specialised pipeline per 64-row block.  Warps 0..7 convert C from
+// FP64 into its digits (the A operand), half a block (32 rows = K16 steps
+// 2h, 2h+1) at a time, into one of two half-buffers, and announce each half
+// on an mbarrier; the loads of the next half are in flight meanwhile.  Warp
+// 8 (one lane) waits for a half, issues its digit-pair MMAs and commits them
+// to that half's "free" barrier, and keeps the V digits (B operand) of the
+// next block arriving by bulk copy into the second of two buffers.  After
+// the last block of a 256-row chunk the converter warps drain the levels
+// into their integer accumulators and release the TMEM to the next chunk.
 struct OzG1Args {
   const double* W0;     // window origin A(j, j)
   long long lda;
@@ -222,14 +224,16 @@ struct OzG1Args {
   BlockState* st;
 };
 
+constexpr int OZ_G1_THREADS = 288;  // 8 converter warps + 1 MMA warp
+
 template <int S>
-__global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
+__global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* adig = base;               // S x 16 KB: 128 C columns x 64 rows
   unsigned char* bdig = base + S * 16384;   // 2 x S x 8 KB: 64 reflectors x 64 rows
   constexpr uint32_t BBYTES = S * 8192;
-  __shared__ uint64_t abar[2], bfull[2];
+  __shared__ uint64_t afull[2], aempty[2], bfull[2], dready, dfree;
   __shared__ uint32_t s_tmem;
   __shared__ int s_e[128];
   const int fjb = g.st->fjb;
@@ -240,178 +244,160 @@ __global__ void __launch_bounds__(OZ_TPB, 1) k_oz_gemm1(OzG1Args g) {
   const int ch_begin = blockIdx.y * g.chunks_per_split;
   const int ch_end = min(nchunk, ch_begin + g.chunks_per_split);
   const int nblk = 4 * max(0, ch_end - ch_begin);
-  const int tid = threadIdx.x;
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
   if (tid < 128) {
     const int c = c0 + tid;
     s_e[tid] = c < g.ncols ? scale_exp_of(g.nrm[c]) : 0;
   }
   if (tid == 0) {
-    tc::mbar_init(&abar[0], 1);
-    tc::mbar_init(&abar[1], 1);
-    tc::mbar_init(&bfull[0], 1);
-    tc::mbar_init(&bfull[1], 1);
-    tc::fence_mbar_init();
-    if (nblk > 0) {
-      tc::mbar_arrive_expect_tx(&bfull[0], BBYTES);
-      tc::bulk_g2s(bdig, g.vb1 + (size_t)(ch_begin * 4) * BBYTES, BBYTES, &bfull[0]);
+    for (int h = 0; h < 2; ++h) {
+      tc::mbar_init(&afull[h], 8);
+      tc::mbar_init(&aempty[h], 1);
+      tc::mbar_init(&bfull[h], 1);
     }
+    tc::mbar_init(&dready, 1);
+    tc::mbar_init(&dfree, 8);
+    tc::fence_mbar_init();
   }
-  if (tid < 32) tc::tmem_alloc(&s_tmem, 512);
+  if (w == 0) tc::tmem_alloc(&s_tmem, 512);
   tc::fence_before_sync();
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
-  const int w = tid >> 5, lane = tid & 31;
-  const int row = 32 * (w & 3) + lane;  // TMEM lane = tile row = C column (c0 + row)
-  const int half = tid >> 7;            // reflector columns [32 half, 32 half + 32)
-  const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
-  long long acc_hi[32];
-  float acc_mid[32];
-#pragma unroll
-  for (int i = 0; i < 32; ++i) {
-    acc_hi[i] = 0;
-    acc_mid[i] = 0.f;
-  }
-  // C rows r0 + 32 h + [0, 32) x columns c0 + [0, 128): 8 row pairs per thread,
-  // 16 consecutive threads on one column (256 contiguous bytes)
-  double2 xv[8];
-  auto load_half = [&](int ib, int h) {
-    const int rb = (ch_begin + (ib >> 2)) * 256 + (ib & 3) * 64 + 32 * h;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int e = tid + OZ_TPB * u;
-      const int rp = e & 15, cc = e >> 4;
-      const int c = c0 + cc, r = rb + 2 * rp;
-      double2 x = make_double2(0.0, 0.0);
-      if (c < g.ncols) {
-        const double* col = g.W0 + (size_t)c * g.lda;
-        if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
-          x = __ldg(reinterpret_cast<const double2*>(col + r));
-        } else {
-          if (r < g.mloc) x.x = __ldg(col + r);
-          if (r + 1 < g.mloc) x.y = __ldg(col + r + 1);
+  bool fail = false;
+  if (w == 8) {
+    // ---------------- MMA issuer and V-digit producer (one lane)
+    if (lane == 0 && nblk > 0) {
+      tc::mbar_arrive_expect_tx(&bfull[0], BBYTES);
+      tc::bulk_g2s(bdig, g.vb1 + (size_t)(ch_begin * 4) * BBYTES, BBYTES, &bfull[0]);
+      for (int ib = 0; ib < nblk; ++ib) {
+        const int kb = ib & 3;
+        const uint32_t bsm = tc::smem_u32(bdig + (ib & 1) * BBYTES);
+        for (int h = 0; h < 2; ++h) {
+          if (!tc::mbar_wait(&afull[h], (uint32_t)(ib & 1))) fail = true;
+          if (h == 0) {
+            if (!tc::mbar_wait(&bfull[ib & 1], (uint32_t)((ib >> 1) & 1))) fail = true;
+            // a chunk's first MMAs overwrite the levels: the previous
+            // chunk must have been drained
+            if (kb == 0 && ib > 0 && !tc::mbar_wait(&dfree, (uint32_t)(((ib >> 2) - 1) & 1))) fail = true;
+          } else if (ib + 1 < nblk) {
+            // every MMA of block ib-1 is complete (its last commit), so the
+            // other B buffer can take block ib+1
+            if (ib >= 1 && !tc::mbar_wait(&aempty[1], (uint32_t)((ib - 1) & 1))) fail = true;
+            const int nb = (ib + 1) & 1;
+            tc::mbar_arrive_expect_tx(&bfull[nb], BBYTES);
+            tc::bulk_g2s(bdig + nb * BBYTES, g.vb1 + (size_t)(ch_begin * 4 + ib + 1) * BBYTES, BBYTES,
+                         &bfull[nb]);
+          }
+          tc::fence_after_sync();
+          if (!fail) oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, bsm, 2 * h, 2 * h + 2, kb == 0 && h == 0);
+          tc::mma_commit(&aempty[h]);
+          if (h == 1 && (kb == 3 || ib == nblk - 1)) tc::mma_commit(&dready);
         }
       }
-      xv[u] = x;
+      // the last commits have landed before the CTA releases TMEM
+      tc::mbar_wait(&aempty[1], (uint32_t)((nblk - 1) & 1));
     }
-  };
-  if (nblk > 0) load_half(0, 0);
-  // failures (a bounded wait that gave up) are per thread and combined at
-  // the next barrier with __syncthreads_or, so every thread leaves together
-  uint32_t aph[2] = {0u, 0u}, bpar[2] = {0u, 0u};
-  bool apend[2] = {false, false};
-  bool bpend[2] = {nblk > 0, false};
-  bool lf = false, ok = true;
-  for (int ib = 0; ib < nblk && ok; ++ib) {
-    const int kb = ib & 3;
+  } else {
+    // ---------------- converters (256 threads) and level drains
+    const int row = 32 * (w & 3) + lane;  // TMEM lane = tile row = C column (c0 + row)
+    const int half = w >> 2;              // reflector columns [32 half, 32 half + 32)
+    const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
+    long long acc_hi[32];
+    float acc_mid[32];
 #pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      // the MMAs that read half h of the A tile (and, for h = 1, every MMA of
-      // the previous block, hence the other B buffer) must be complete
-      if (apend[h]) {
-        if (!tc::mbar_wait(&abar[h], aph[h])) lf = true;
-        aph[h] ^= 1u;
-        apend[h] = false;
-      }
-      if (h == 1 && ib + 1 < nblk) {
-        const int nb = (ib + 1) & 1;
-        if (tid == 0) {
-          tc::mbar_arrive_expect_tx(&bfull[nb], BBYTES);
-          tc::bulk_g2s(bdig + nb * BBYTES, g.vb1 + (size_t)(ch_begin * 4 + ib + 1) * BBYTES, BBYTES,
-                       &bfull[nb]);
-        }
-        bpend[nb] = true;
-        bpar[nb] = (uint32_t)(((ib + 1) >> 1) & 1);
-      }
+    for (int i = 0; i < 32; ++i) {
+      acc_hi[i] = 0;
+      acc_mid[i] = 0.f;
+    }
+    // C rows r0 + 32 h + [0, 32) x columns c0 + [0, 128): 8 row pairs per
+    // thread, 16 consecutive threads on one column (256 contiguous bytes)
+    double2 xv[8];
+    auto load_half = [&](int ib, int h) {
+      const int rb = (ch_begin + (ib >> 2)) * 256 + (ib & 3) * 64 + 32 * h;
 #pragma unroll
       for (int u = 0; u < 8; ++u) {
-        const int e = tid + OZ_TPB * u;
+        const int e = tid + 256 * u;
         const int rp = e & 15, cc = e >> 4;
-        const int sh = 8 * S - s_e[cc];
-        int d0[S], d1[S];
-        balanced_digits<S>(fixed_point(xv[u].x, sh), d0);
-        balanced_digits<S>(fixed_point(xv[u].y, sh), d1);
-        const uint32_t off = tc::sw128_offset(cc, 32 * h + 2 * rp);
+        const int c = c0 + cc, r = rb + 2 * rp;
+        double2 x = make_double2(0.0, 0.0);
+        if (c < g.ncols) {
+          const double* col = g.W0 + (size_t)c * g.lda;
+          if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
+            x = __ldg(reinterpret_cast<const double2*>(col + r));
+          } else {
+            if (r < g.mloc) x.x = __ldg(col + r);
+            if (r + 1 < g.mloc) x.y = __ldg(col + r + 1);
+          }
+        }
+        xv[u] = x;
+      }
+    };
+    if (nblk > 0) load_half(0, 0);
+    for (int ib = 0; ib < nblk; ++ib) {
+      const int kb = ib & 3;
 #pragma unroll
-        for (int p = 0; p < S; ++p)
-          *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+      for (int h = 0; h < 2; ++h) {
+        // the MMAs that read this half for the previous block are complete
+        if (ib >= 1 && !tc::mbar_wait(&aempty[h], (uint32_t)((ib - 1) & 1))) fail = true;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = tid + 256 * u;
+          const int rp = e & 15, cc = e >> 4;
+          const int sh = 8 * S - s_e[cc];
+          int d0[S], d1[S];
+          balanced_digits<S>(fixed_point(xv[u].x, sh), d0);
+          balanced_digits<S>(fixed_point(xv[u].y, sh), d1);
+          const uint32_t off = tc::sw128_offset(cc, 32 * h + 2 * rp);
+#pragma unroll
+          for (int p = 0; p < S; ++p)
+            *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+        }
+        tc::fence_async_smem();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&afull[h]);
+        // C of the next half, in flight while this half is multiplied
+        if (h == 0) load_half(ib, 1);
+        else if (ib + 1 < nblk) load_half(ib + 1, 0);
       }
-      // C of the next half, in flight while this half is multiplied
-      if (h == 0) load_half(ib, 1);
-      else if (ib + 1 < nblk) load_half(ib + 1, 0);
-      tc::fence_async_smem();
-      if (__syncthreads_or(lf)) {
-        ok = false;
-        break;
-      }
-      if (tid == 0) {
+      if (kb == 3 || ib == nblk - 1) {
+        // end of a 256-row chunk: drain the levels into the accumulators
+        if (!tc::mbar_wait(&dready, (uint32_t)((ib >> 2) & 1))) fail = true;
         tc::fence_after_sync();
-        bool ready = true;
-        if (h == 0) {
-          ready = tc::mbar_wait(&bfull[ib & 1], bpar[ib & 1]);
-          if (!ready) lf = true;
+#pragma unroll
+        for (int g8 = 0; g8 < 4; ++g8) {
+          long long hi[8], mid[8];
+          oz_levels8<S>(taddr, 32 * half + 8 * g8, hi, mid);
+#pragma unroll
+          for (int i = 0; i < 8; ++i) {
+            acc_hi[8 * g8 + i] += hi[i];
+            acc_mid[8 * g8 + i] += (float)mid[i];
+          }
         }
-        if (ready)
-          oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, tc::smem_u32(bdig + (ib & 1) * BBYTES), 2 * h, 2 * h + 2,
-                      kb == 0 && h == 0);
-        tc::mma_commit(&abar[h]);
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive(&dfree);
       }
-      if (h == 0) bpend[ib & 1] = false;
-      apend[h] = true;
     }
-    if (!ok) break;
-    if (kb == 3 || ib == nblk - 1) {
-      // end of a 256-row chunk: drain the levels into the integer accumulators
+    if (!fail) {
+      // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1))
+      const int c = c0 + row;
+      double* out = g.Wp + ((size_t)blockIdx.y * g.npad + (size_t)(c - fjb)) * 64;
+      if (c < g.ncols) {
+        const int e = s_e[row];
 #pragma unroll
-      for (int h = 0; h < 2; ++h)
-        if (apend[h]) {
-          if (!tc::mbar_wait(&abar[h], aph[h])) lf = true;
-          aph[h] ^= 1u;
-          apend[h] = false;
+        for (int i = 0; i < 32; ++i) {
+          const int a = 32 * half + i;
+          double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
+          out[a] = a < k ? v : 0.0;
         }
-      tc::fence_after_sync();
-#pragma unroll
-      for (int g8 = 0; g8 < 4; ++g8) {
-        long long hi[8], mid[8];
-        oz_levels8<S>(taddr, 32 * half + 8 * g8, hi, mid);
-#pragma unroll
-        for (int i = 0; i < 8; ++i) {
-          acc_hi[8 * g8 + i] += hi[i];
-          acc_mid[8 * g8 + i] += (float)mid[i];
-        }
-      }
-      tc::fence_before_sync();
-      if (__syncthreads_or(lf)) ok = false;
-    }
-  }
-  // on failure: let the commits and copies still in flight land before the
-  // shared memory and TMEM are released (bounded waits)
-#pragma unroll
-  for (int h = 0; h < 2; ++h)
-    if (apend[h]) tc::mbar_wait(&abar[h], aph[h]);
-  if (tid == 0) {
-    for (int b = 0; b < 2; ++b)
-      if (bpend[b]) tc::mbar_wait(&bfull[b], bpar[b]);
-  }
-  if (!ok) {
-    if (tid == 0) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
-  } else {
-    // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1))
-    const int c = c0 + row;
-    double* out = g.Wp + ((size_t)blockIdx.y * g.npad + (size_t)(c - fjb)) * 64;
-    if (c < g.ncols) {
-      const int e = s_e[row];
-#pragma unroll
-      for (int i = 0; i < 32; ++i) {
-        const int a = 32 * half + i;
-        double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
-        out[a] = a < k ? v : 0.0;
       }
     }
   }
+  if (fail) atomicOr(&g.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
   tc::fence_before_sync();
   __syncthreads();
-  if (tid < 32) tc::tmem_dealloc(tmem, 512);
+  if (w == 0) tc::tmem_dealloc(tmem, 512);
 }
 
 // ------------------------------------------- W2 = T^T W and its digits
@@ -716,7 +702,7 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
   a1.Wp = Wp;
   a1.npad = npad;
   a1.st = st;
-  k_oz_gemm1<S><<<dim3(ctiles, nsplit), OZ_TPB, oz_gemm1_smem(S), st_>>>(a1);
+  k_oz_gemm1<S><<<dim3(ctiles, nsplit), OZ_G1_THREADS, oz_gemm1_smem(S), st_>>>(a1);
   k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nsplit, npad, T, ldt, ncols, st, wb2, wexp);
   OzG2Args a2;
   a2.W0 = W0;
