@@ -173,6 +173,32 @@ __device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32
 // Load the S levels of 8 accumulator columns (col0..col0+7) of this thread's
 // TMEM lane and combine them: hi = sum_{L<=5} D_L 2^(8(5-L)) (exact int64),
 // mid = sum_{L>=6} D_L 2^(8(S+1-L)) (int64 of exact or nearly exact values).
+// GEMM2 layout: level L at columns (L - 2) * 32 + col of one 256-column buffer
+template <int S>
+__device__ __forceinline__ void oz_levels8(uint32_t taddr_buf, int, long long* hi, long long* mid, uint32_t col) {
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    hi[i] = 0;
+    mid[i] = 0;
+  }
+#pragma unroll
+  for (int L = 2; L <= S + 1; ++L) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr_buf + (uint32_t)((L - 2) * 32) + col)
+                 : "memory");
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      long long v = (long long)f32_to_int(__uint_as_float(r[i]));
+      if (L <= 5) hi[i] += v << (8 * (5 - L));
+      else mid[i] += v << (8 * (S + 1 - L));
+    }
+  }
+}
+
 template <int S>
 __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long long* hi, long long* mid) {
 #pragma unroll
@@ -444,12 +470,14 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
     sT[a][b] = (a < k && b < k) ? T[(size_t)a * ldt + b] : 0.0;
   }
   __syncthreads();
-  // W2(a, c) = sum_{b <= a} T(b, a) W(b, c)
+  // W2(a, c) = sum_{b <= a} T(b, a) W(b, c); a warp's lanes share two
+  // values of a, so their loops have (nearly) equal trip counts (an FP64
+  // warp instruction costs the same whatever its active lanes)
   double w2[4];
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int e = threadIdx.x + OZ_TPB * i;  // 0..1023
-    const int cc = e / 64, a = e % 64;
+    const int a = e >> 4, cc = e & 15;
     double acc = 0.0;
     if (a < k)
       for (int b = 0; b <= a; ++b) acc = fma(sT[a][b], sW[cc][b], acc);
@@ -459,7 +487,7 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
 #pragma unroll
   for (int i = 0; i < 4; ++i) {
     const int e = threadIdx.x + OZ_TPB * i;
-    sW[e / 64][e % 64] = w2[i];
+    sW[e & 15][e >> 4] = w2[i];
   }
   __syncthreads();
   if (threadIdx.x < OZ_W2_COLS) {
@@ -598,7 +626,8 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
         tc::mbar_wait(&empty[kk % NST2], (uint32_t)((kk / NST2) & 1));
     }
   } else {
-    // epilogue: rows 32 (w & 3) + lane of the band, columns 16 (w >> 2) + j
+    // epilogue: rows 32 (w & 3) + lane of the band, columns 16 (w >> 2) + j,
+    // in two groups of 8 columns
     const int quad = w & 3, ch = w >> 2;
     const uint32_t tl = tmem + ((uint32_t)(32 * quad) << 16);
     for (int kk = 0; kk < nmine; ++kk) {
@@ -613,40 +642,30 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
       }
       if (!tc::mbar_wait(&tfull[b], (uint32_t)((kk >> 1) & 1))) fail = true;
       tc::fence_after_sync();
-      long long hi[16], mid[16];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        hi[j] = 0;
-        mid[j] = 0;
-      }
-#pragma unroll
-      for (int L = 2; L <= S + 1; ++L) {
-        float v[16];
-        tc::tmem_ld16(tl + (uint32_t)(b * 256 + (L - 2) * 32 + 16 * ch), v);
-        tc::tmem_wait_ld();
-#pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const long long x = (long long)f32_to_int(v[j]);
-          if (L <= 5) hi[j] += x << (8 * (5 - L));
-          else mid[j] += x << (8 * (S + 1 - L));
+      for (int jb = 0; jb < 16; jb += 8) {
+        long long hi[8], mid[8];
+        oz_levels8<S>(tl + (uint32_t)(b * 256), 0, hi, mid, (uint32_t)(16 * ch + jb));
+        if (jb == 8) {
+          tc::fence_before_sync();
+          __syncwarp();
+          if (lane == 0) tc::mbar_arrive(&tempty[b]);
         }
-      }
-      tc::fence_before_sync();
-      __syncwarp();
-      if (lane == 0) tc::mbar_arrive(&tempty[b]);
-      if (!fail && r < g.mloc) {
+        if (!fail && r < g.mloc) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const int cw = cw0 + j, c = fjb + cw;
-          if (c < g.ncols) {
-            const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
-            // U = 2^e (hi 256^-5 + mid 256^-(S+1)).  hi < 2^45 and mid <
-            // 2^40, so hi 2^17 + mid 2^(57-8S) fits in 62 bits and keeps
-            // ~2^-62 of U; the power-of-two scale is exact, so one FMA rounds
-            // once, as a multiply and a subtraction would.
-            constexpr int msh = 8 * (S + 1) - 40 - 17;
-            const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
-            g.W0[(size_t)c * g.lda + r] = fma(-(double)comb, pow2d(e - 40 - 17), cv[j]);
+          for (int j = 0; j < 8; ++j) {
+            const int cw = cw0 + jb + j, c = fjb + cw;
+            if (c < g.ncols) {
+              // U = 2^e (hi 256^-5 + mid 256^-(S+1)) = comb 2^(e-57): hi < 2^45
+              // and mid < 2^40, so hi 2^17 + mid 2^(57-8S) fits in 62 bits and
+              // keeps ~2^-62 of U; the power-of-two scale is exact, so one FMA
+              // rounds once, as a multiply and a subtraction would
+              const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
+              constexpr int msh = 8 * (S + 1) - 40 - 17;
+              const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
+              const double res = fma(-(double)comb, pow2d(e - 57), cv[jb + j]);
+              g.W0[(size_t)c * g.lda + r] = res;
+            }
           }
         }
       }
