@@ -50,7 +50,11 @@ WORKLOADS = {
     "kahan4k": (4096, 4096, "Kahan c=0.285 + 1e-14 N(0,1)"),
     "graded1k": (1000, 1000, "U diag(10^(-12(i-1)/999)) V^T"),
     "batched2000": (0, 0, "2000 uneven U diag(s) V^T, n in [32, 512], m = n r, r in [1, 4]"),
+    "select32k": (8192, 32768, "selection stress: 4096 N(0,1) base columns repeated U{1..8} times "
+                               "(1e-8 relative perturbation), filler N(0,1) 10^-U[0,6], shuffled"),
 }
+KSTOP = {"select32k": 4096}  # column-subset selection: stop after k columns
+SELECTION_BASES = {}
 BATCH_COUNT, BATCH_NB = 2000, 32
 BATCH_GENERATOR = None
 BATCH_CPU_SAMPLE = 400
@@ -81,6 +85,12 @@ def make_matrix_device(name, seed=3):
         at = rf @ lf.T
         at += 1e-10 * torch.randn(n, m, generator=g, dtype=torch.float64, device=dev)
         return at.contiguous()
+    if name == "select32k":
+        from qrdm_gb300 import workloads as W
+
+        a, bid = W.selection_stress(m, n, 4096, seed=5, return_base=True)
+        SELECTION_BASES[name] = bid
+        return torch.from_numpy(np.ascontiguousarray(a.T)).to(dev)
     from qrdm_gb300 import workloads as W
 
     if name == "gauss4k":
@@ -275,7 +285,7 @@ def run_ours(args):
         work.copy_(pristine)
         jp.zero_()
         nc = np.zeros(n, np.int32)
-        opt = default_options(precision=precision)
+        opt = default_options(precision=precision, kstop=KSTOP.get(args.workload, 0))
         st = stats if stats is not None else Stats()
         info = L.dgeqrdm_dev(102, m, n, C.c_void_p(work.data_ptr()), m, C.c_void_p(jp.data_ptr()),
                              C.c_void_p(tau.data_ptr()), nc.ctypes.data_as(C.POINTER(C.c_int)),
@@ -303,7 +313,12 @@ def run_ours(args):
         barrier(world)
     ms = ev0.elapsed_time(ev1) / args.steps
     ms = max_over_ranks(ms, world)
-    F = flops_full(m, n)
+    kst = KSTOP.get(args.workload, 0)
+    if kst:
+        kdone = int(np.sum(nc[:int(np.count_nonzero(nc))]))
+        F = flops_k(m, n, kdone) if kdone < min(m, n) else flops_full(m, n)
+    else:
+        F = flops_full(m, n)
     value = world * F / (ms / 1e3) / 1e12
     clocks = clk.summary()
 
@@ -363,7 +378,7 @@ def run_ours(args):
             a_np[...] = src
             jp_h[:] = 0
             nc = np.zeros(n, np.int32)
-            opt = default_options(precision=prec)
+            opt = default_options(precision=prec, kstop=KSTOP.get(args.workload, 0))
             st = Stats()
             t0 = time.perf_counter()
             info = L.dgeqrdm_ex(102, m, n, a_np.ctypes.data_as(pd), m,
@@ -383,6 +398,16 @@ def run_ours(args):
                 step(st64, precision=0)
                 variants["fp64_dmqr_ms"] = st64.ms_total
                 variants["fp64_dmqr_tflops"] = F / (st64.ms_total / 1e3) / 1e12
+            if args.workload in SELECTION_BASES:
+                # selection property: no base column chosen twice among the first k
+                step(precision=prec)
+                bid = SELECTION_BASES[args.workload]
+                k = KSTOP[args.workload]
+                sel = bid[jp[:k].cpu().numpy().astype(np.int64) - 1]
+                sel = sel[sel >= 0]
+                variants["selected_bases"] = int(len(sel))
+                variants["distinct_bases"] = bool(len(np.unique(sel)) == len(sel))
+        if args.variants and args.workload not in KSTOP:
             # GPU QP3 (dgeqp3 semantics) on the same matrix, one run
             work.copy_(pristine)
             jp.zero_()
@@ -397,6 +422,7 @@ def run_ours(args):
                 variants["qp3_ms"] = q0.elapsed_time(q1)
                 variants["qp3_tflops"] = F / (variants["qp3_ms"] / 1e3) / 1e12
                 variants["speedup_vs_qp3"] = variants["qp3_ms"] / ms
+        if args.variants:
             if "fp64_dmqr_ms" in variants:
                 variants["speedup_vs_fp64"] = variants["fp64_dmqr_ms"] / ms
             variants["phase_ms"] = phase
@@ -415,6 +441,7 @@ def run_ours(args):
                "data": "synthetic",
                "config": {"workload": args.workload, "m": m, "n": n, "nb": NB, "delta": DELTA,
                           "tau_": TAU_, "precision": args.precision, "matrix": desc,
+                          "kstop": KSTOP.get(args.workload, 0),
                           "parallelism": f"replicas{world}",
                           "l2": "inputs (8 m n bytes) larger than L2; no flush needed"},
                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,

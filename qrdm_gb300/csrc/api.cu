@@ -1061,7 +1061,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   std::stable_sort(work.begin(), work.end());
   for (int i = 0; i < count; ++i) ho[i] = work[i].second;
   const size_t meta_bytes = sizeof(long long) * count + sizeof(int) * meta.size() + sizeof(int) * 4;
-  const int grid = c->nsm;
+  const int grid = c->nsm * batched_ctas_per_sm(nb);
   const long long wsd = batched_ws_doubles(nmax);
   unsigned long long key = 1469598103934665603ull;
   key = fnv1a(key, meta.data(), sizeof(int) * meta.size());
@@ -1109,6 +1109,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   L.queue = d_queue;
   L.prof = c->b_prof.as<unsigned long long>();
   L.grid = grid;
+  c->b_grid = grid;
   // capture the reset + launch once; later identical calls replay it
   if (c->b_graph) {
     cudaGraphExecDestroy(c->b_graph);
@@ -1151,7 +1152,8 @@ int qrdm_batched_phase_cycles(unsigned long long* out, int nout) {
   const int ph = batched_phases();
   for (int k = 0; k < nout; ++k) out[k] = 0;
   if (!c->b_prof.p) return 0;
-  const int grid = c->nsm;
+  const int grid = c->b_grid;
+  if (grid <= 0) return 0;
   std::vector<unsigned long long> h((size_t)grid * ph);
   CK(cudaMemcpyAsync(h.data(), c->b_prof.p, sizeof(unsigned long long) * h.size(), cudaMemcpyDeviceToHost,
                      c->stream()));

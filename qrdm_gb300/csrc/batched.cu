@@ -26,18 +26,19 @@ constexpr int BKMAX = 64;          // largest DM block of a batched problem
 // update, CW = 4096 / KW, KW in {32, 64}; also the Gram and swap staging
 constexpr int kStage = 32 * 33 + 32 * 129 + 32;
 
+template <int KB>
 struct BatchShared {
   Cand cand[BNMAX];
-  double g[64 * 65];        // cosine Gram / V^T V
-  double T[64 * 64];
+  double g[KB * (KB + 1)];  // cosine Gram / V^T V (row stride KB + 1)
+  double T[KB * KB];
   double stage[kStage];     // row tiles of the GEMM operands
   double red[BT];
-  double tw[BKMAX];
-  double sc[BKMAX];
-  double jv_n[4 * BKMAX + 8];
-  int jv_j[4 * BKMAX + 8];
-  int2 perm[4 * BKMAX + 8];
-  int sel[BKMAX], pos[BKMAX], swa[2 * BKMAX + 2], swb[2 * BKMAX + 2];
+  double tw[KB];
+  double sc[KB];
+  double jv_n[4 * KB + 8];
+  int jv_j[4 * KB + 8];
+  int2 perm[4 * KB + 8];
+  int sel[KB], pos[KB], swa[2 * KB + 2], swb[2 * KB + 2];
   unsigned bits[BNMAX / 32];
   int list[BNMAX];
   double maxv, eta, alpha, tau, scal, beta, thres;
@@ -86,9 +87,9 @@ __device__ __forceinline__ double pow2_for(double nrm) {
 
 // G[p][q] = sum_{r in [0, len)} f(r, p) f(r, q), p, q < KW (32 or 64), via
 // (2048 / KW)-row shared-memory stages and (KW/16) x (KW/16) register tiles
-// (256 threads).  Result in g (row stride 65).
+// (256 threads).  Result in g (row stride gs).
 template <int KW, class F>
-__device__ void cta_gram(int len, F f, double* stage, double* g) {
+__device__ void cta_gram(int len, F f, double* stage, double* g, int gs) {
   constexpr int RS = 2048 / KW;  // rows per stage
   constexpr int TT = KW / 16;    // register tile edge
   constexpr int LD = KW + 1;
@@ -122,14 +123,14 @@ __device__ void cta_gram(int len, F f, double* stage, double* g) {
 #pragma unroll
   for (int a = 0; a < TT; ++a)
 #pragma unroll
-    for (int b = 0; b < TT; ++b) g[(tp + 16 * a) * 65 + tq + 16 * b] = acc[a][b];
+    for (int b = 0; b < TT; ++b) g[(tp + 16 * a) * gs + tq + 16 * b] = acc[a][b];
   __syncthreads();
 }
 
-template <class F>
+template <int KB, class F>
 __device__ void cta_gram_any(int k, int len, F f, double* stage, double* g) {
-  if (k <= 32) cta_gram<32>(len, f, stage, g);
-  else cta_gram<64>(len, f, stage, g);
+  if (KB == 32 || k <= 32) cta_gram<32>(len, f, stage, g, KB + 1);
+  else cta_gram<64>(len, f, stage, g, KB + 1);
 }
 
 // Trailing update of one DM block: C <- C - V (T^T (V^T C)) for the n2
@@ -139,7 +140,7 @@ __device__ void cta_gram_any(int k, int len, F f, double* stage, double* g) {
 // [64][n]) subtracted in 64 x 64 tiles.
 template <int KW>
 __device__ void cta_trailing(const double* V0, double* C0, long long lda, int mloc, int kc, int n2, int n,
-                             const double* T, double* g, double* stage, double* W) {
+                             const double* T, int ldt, double* stage, double* W) {
   constexpr int CW = 4096 / KW;
   constexpr int NTC = CW / 4;  // threads along the columns
   constexpr int LV = KW + 1, LC = CW + 1;
@@ -180,6 +181,7 @@ __device__ void cta_trailing(const double* V0, double* C0, long long lda, int ml
       }
       __syncthreads();
     }
+    double* g = stage;  // the V^T C tile, KW x CW (row stride LC)
 #pragma unroll
     for (int x = 0; x < 4; ++x)
 #pragma unroll
@@ -191,7 +193,7 @@ __device__ void cta_trailing(const double* V0, double* C0, long long lda, int ml
       if (c0 + cc >= n2) continue;
       double s2 = 0.0;
       if (aa < kc)
-        for (int b = 0; b <= aa; ++b) s2 = fma(T[aa * 64 + b], g[b * LC + cc], s2);
+        for (int b = 0; b <= aa; ++b) s2 = fma(T[aa * ldt + b], g[b * LC + cc], s2);
       W[(size_t)aa * n + c0 + cc] = s2;
     }
     __syncthreads();
@@ -276,8 +278,10 @@ constexpr int kPhases = 8;
     }                                            \
   } while (0)
 
-__device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
+template <int KB>
+__device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double* ws,
                           unsigned long long* pacc) {
+  constexpr int GS = KB + 1;
   const int m = a.m[p], n = a.n[p];
   double* A = a.A + a.a_off[p];
   const long long lda = m;
@@ -362,12 +366,12 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
     const int nc = S.nc;
     // ---- cosine Gram of the scaled candidates
     if (nc > 1) {
-      if (tid < 64) S.tw[tid] = tid < nc ? 1.0 / S.cand[tid].val : 0.0;
+      if (tid < KB) S.tw[tid] = tid < nc ? 1.0 / S.cand[tid].val : 0.0;
       __syncthreads();
       auto f = [&](int r, int q) -> double {
         return q < nc ? S.tw[q] * W0[(size_t)S.cand[q].idx * lda + r] : 0.0;
       };
-      cta_gram_any(nc, mloc, f, S.stage, S.g);
+      cta_gram_any<KB>(nc, mloc, f, S.stage, S.g);
     }
     // ---- greedy pick (warp 0) and permute_marked replay (thread 0)
     const int nwords = (nloc + 31) >> 5;
@@ -382,7 +386,7 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
       __syncwarp();
       for (int i = 1; i < nc; ++i) {
         double worst = 0.0;
-        for (int q = lane; q < nsel; q += 32) worst = fmax(worst, fabs(S.g[S.pos[q] * 65 + i]));
+        for (int q = lane; q < nsel; q += 32) worst = fmax(worst, fabs(S.g[S.pos[q] * GS + i]));
         worst = warp_max(worst);
         if (worst < a.delta && nsel < kmax) {
           if (lane == 0) {
@@ -401,7 +405,7 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
       unsigned* bits = S.bits;
       for (int q = 0; q < nsel; ++q) bits[S.sel[q] >> 5] |= 1u << (S.sel[q] & 31);
 #define BMARK(x) ((bits[(x) >> 5] >> ((x) & 31)) & 1u)
-      const int maxsw = 2 * BKMAX + 2;
+      const int maxsw = 2 * KB + 2;
       int nswap = 0, jb = 0, jt = nloc - 1;
       auto xchg = [&](int x, int y) {
         if (BMARK(x) != BMARK(y)) {
@@ -560,23 +564,23 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
       auto fv = [&](int r, int q) -> double {
         return q < kc ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
       };
-      cta_gram_any(kc, mloc, fv, S.stage, S.g);
+      cta_gram_any<KB>(kc, mloc, fv, S.stage, S.g);
     }
-    for (int e = tid; e < 64 * 64; e += blockDim.x) S.T[e] = 0.0;
+    for (int e = tid; e < KB * KB; e += blockDim.x) S.T[e] = 0.0;
     __syncthreads();
     {
       const int ar = tid >> 2, part = tid & 3;
       for (int i = 0; i < kc; ++i) {
         const double ti = tau[j + i];
-        if (tid < i) S.red[tid] = -ti * S.g[tid * 65 + i];
+        if (tid < i) S.red[tid] = -ti * S.g[tid * GS + i];
         __syncthreads();
         double acc = 0.0;
         if (ar < i && ti != 0.0)
-          for (int b = ar + part; b < i; b += 4) acc = fma(S.T[b * 64 + ar], S.red[b], acc);
+          for (int b = ar + part; b < i; b += 4) acc = fma(S.T[b * KB + ar], S.red[b], acc);
         acc += __shfl_xor_sync(0xffffffffu, acc, 1);
         acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-        if (ar < i && part == 0) S.T[i * 64 + ar] = acc;
-        if (tid == 0) S.T[i * 64 + i] = ti;
+        if (ar < i && part == 0) S.T[i * KB + ar] = acc;
+        if (tid == 0) S.T[i * KB + i] = ti;
         __syncthreads();
       }
     }
@@ -585,8 +589,10 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
     // ---- trailing update C <- (I - V T V^T)^T C, C = window columns fjb..
     const int n2 = nloc - fjb;
     if (kc > 0 && n2 > 0) {
-      if (kc <= 32) cta_trailing<32>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, S.g, S.stage, W);
-      else cta_trailing<64>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, S.g, S.stage, W);
+      if (KB == 32 || kc <= 32)
+        cta_trailing<32>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, KB, S.stage, W);
+      else
+        cta_trailing<64>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, KB, S.stage, W);
     }
     __syncthreads();
     BPH(4);
@@ -651,9 +657,12 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared& S, double* ws,
   if (tid == 0 && a.info) a.info[p] = 0;
 }
 
-__global__ void __launch_bounds__(BT, 1) k_dmqr_batched(BatchArgs a) {
+// KB = 32: blocks of at most 32 columns (smem ~85 KB, <= 128 registers);
+// KB = 64: blocks of up to 64 columns.
+template <int KB>
+__global__ void __launch_bounds__(BT, KB == 32 ? 2 : 1) k_dmqr_batched(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  BatchShared& S = *reinterpret_cast<BatchShared*>(smem_raw);
+  BatchShared<KB>& S = *reinterpret_cast<BatchShared<KB>*>(smem_raw);
   double* ws = a.ws + (size_t)blockIdx.x * a.ws_stride;
   const int tid = threadIdx.x;
   unsigned long long pacc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -666,7 +675,7 @@ __global__ void __launch_bounds__(BT, 1) k_dmqr_batched(BatchArgs a) {
     __syncthreads();
     BPH(6);
     if (q >= a.count) break;
-    solve_one(a, a.order[q], S, ws, pacc);
+    solve_one<KB>(a, a.order[q], S, ws, pacc);
     __syncthreads();
   }
   if (a.prof && tid == 0) {
@@ -675,15 +684,21 @@ __global__ void __launch_bounds__(BT, 1) k_dmqr_batched(BatchArgs a) {
   }
 }
 
-size_t batched_smem_bytes() { return sizeof(BatchShared); }
+size_t batched_smem_bytes(int nb) { return nb <= 32 ? sizeof(BatchShared<32>) : sizeof(BatchShared<64>); }
+// One CTA per SM for both widths: two CTAs sharing an SM's FP64 pipe
+// lengthen the largest problems (which start first) and so the makespan.
+int batched_ctas_per_sm(int) { return 1; }
 int batched_phases() { return kPhases; }
 int batched_nmax() { return BNMAX; }
 int batched_kmax() { return BKMAX; }
 long long batched_ws_doubles(int nmax) { return 2LL * BNMAX + 64LL * nmax; }
 
 int batched_set_attributes() {
-  return cudaFuncSetAttribute(k_dmqr_batched, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)sizeof(BatchShared)) == cudaSuccess ? 0 : 1;
+  if (cudaFuncSetAttribute(k_dmqr_batched<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sizeof(BatchShared<32>)) != cudaSuccess)
+    return 1;
+  return cudaFuncSetAttribute(k_dmqr_batched<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)sizeof(BatchShared<64>)) == cudaSuccess ? 0 : 1;
 }
 
 // Enqueue the persistent batched kernel (queue counter reset + launch).
@@ -711,7 +726,8 @@ int launch_batched(const BatchLaunch& L, cudaStream_t s) {
   a.queue = L.queue;
   a.prof = L.prof;
   if (cudaMemsetAsync(L.queue, 0, sizeof(int), s) != cudaSuccess) return 1;
-  k_dmqr_batched<<<L.grid, BT, sizeof(BatchShared), s>>>(a);
+  if (L.nb <= 32) k_dmqr_batched<32><<<L.grid, BT, sizeof(BatchShared<32>), s>>>(a);
+  else k_dmqr_batched<64><<<L.grid, BT, sizeof(BatchShared<64>), s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 

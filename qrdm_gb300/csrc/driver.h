@@ -55,6 +55,7 @@ struct Ctx {
   Buf b_meta, b_ws, b_prof;                     // batched DM-QR
   Buf pan_prof;                                 // clustered panel phase cycles (timing runs)
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch
+  int b_grid = 0;                               // CTAs of the last batched launch
   unsigned long long b_key = 0;
   BlockState* h_st = nullptr;              // pinned host copy of the block record
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -125,7 +125,8 @@ struct BatchLaunch {
 int batched_set_attributes();
 int batched_phases();
 int launch_batched(const BatchLaunch& L, cudaStream_t s);
-size_t batched_smem_bytes();
+size_t batched_smem_bytes(int nb);
+int batched_ctas_per_sm(int nb);
 int batched_nmax();
 int batched_kmax();
 long long batched_ws_doubles(int nmax);

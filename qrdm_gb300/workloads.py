@@ -76,11 +76,12 @@ def low_rank_noise(m: int = 16384, n: int = 8192, r: int = 2048, noise: float = 
 
 
 def selection_stress(m: int = 8192, n: int = 32768, nbase: int = 4096, seed: int = 5,
-                     rel: float = 1e-8) -> np.ndarray:
+                     rel: float = 1e-8, return_base: bool = False):
     """Column-subset-selection stress matrix: nbase N(0,1) base columns, each
     repeated U{1..8} times with a (1 + rel * N(0,1)) entrywise perturbation,
     the rest N(0,1) * 10^(-u), u ~ U[0,6]; truncated/filled to n columns and
-    shuffled by seed."""
+    shuffled by seed.  return_base: also the base index of every column
+    (-1 for the filler columns)."""
     rng = np.random.default_rng(seed)
     base = rng.standard_normal((m, nbase))
     reps = rng.integers(1, 9, size=nbase)
@@ -99,6 +100,10 @@ def selection_stress(m: int = 8192, n: int = 32768, nbase: int = 4096, seed: int
         u = rng.uniform(0.0, 6.0)
         a[:, t] = rng.standard_normal(m) * 10.0 ** (-u)
     perm = rng.permutation(n)
+    if return_base:
+        bid = np.full(n, -1, np.int64)
+        bid[:len(cols)] = [j for j, _ in cols]
+        return np.asfortranarray(a[:, perm]), bid[perm]
     return np.asfortranarray(a[:, perm])
 
 
