@@ -563,7 +563,7 @@ def run_batched(args):
 
     def step():
         b.a.copy_(pristine)
-        r = b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+        r = b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_, precision=args.precision)
         if r != 0:
             raise RuntimeError(f"dgeqrdm_batched_dev returned {r}")
 
@@ -594,7 +594,7 @@ def run_batched(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+        b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_, precision=args.precision)
         e1.record(stream)
         torch.cuda.synchronize()
         kms = e0.elapsed_time(e1)
@@ -610,7 +610,8 @@ def run_batched(args):
         except RuntimeError:  # torch's GPU linear algebra unavailable
             be, orth = np.full(1, np.nan), np.full(1, np.nan)
         achieved = F / (kms / 1e3) / 1e12
-        roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch)",
+        roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch; trailing update "
+                "on " + ("BF16 tensor cores, Ozaki split" if args.precision == "mixed" else "FP64") + ")",
                 "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
                 "peak_kind": "nominal FP64 (no measured FP64 peak); HBM term from measured "
                              f"{peaks['hbm_gbs']} GB/s", "unit": "TFLOP/s",
@@ -627,7 +628,7 @@ def run_batched(args):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             b.a.copy_(host, non_blocking=True)
-            b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+            b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_, precision=args.precision)
             back.copy_(b.a, non_blocking=True)
             jp_h = b.jpvt.cpu()
             tau_h = b.tau.cpu()
@@ -649,6 +650,7 @@ def run_batched(args):
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic",
                "config": {"workload": "batched2000", "count": count, "nb": BATCH_NB,
+                          "precision": args.precision,
                           "delta": DELTA, "tau_": TAU_, "flops": F, "generator": BATCH_GENERATOR,
                           "bytes": 8 * pristine.numel(),
                           "parallelism": f"replicas{world}",

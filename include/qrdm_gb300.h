@@ -120,10 +120,12 @@ int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda, i
  *           zero after the last block), d_tau sum min(m_i, n_i) doubles,
  *           d_info count ints (0 or -13) or NULL.
  * thres = [delta, tau_, eta] (host), stop = the stop mode of dgeqrdm's
- * ncols[0] (0..3) for every problem, nb <= 64.  Repeated calls with the same
- * description replay a captured CUDA graph. */
+ * ncols[0] (0..3) for every problem, nb <= 64.  precision: 0 = FP64, 1 =
+ * trailing update on the BF16 tensor cores with the Ozaki split (FP64
+ * accuracy; nb <= 32).  Repeated calls with the same description replay a
+ * captured CUDA graph. */
 int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int* d_jpvt, double* d_tau,
-                        int* d_ncols, int* d_info, const double* thres, int stop, int nb);
+                        int* d_ncols, int* d_info, const double* thres, int stop, int nb, int precision);
 
 /* Device cycles spent by the last dgeqrdm_batched_dev call, summed over its
  * CTAs: out[0..7] = norms, selection, panel, T factor, trailing update,
@@ -160,8 +162,9 @@ int qrdm_dormqr_dev(int matrix_layout, int m, int n, int k, const double* d_a, i
                     const double* d_tau, double* d_c, int ldc);
 
 /* ------------------------------------------------------------- runtime */
-/* Make subsequent calls run on this cudaStream_t (NULL: the library's own
- * stream).  Returns 0. */
+/* Make subsequent calls run on this cudaStream_t (NULL, the default: the
+ * legacy default stream, ordered with the caller's other blocking streams).
+ * Returns 0. */
 int qrdm_set_stream(void* stream);
 /* Human-readable build identification. */
 const char* qrdm_version(void);

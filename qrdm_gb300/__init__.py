@@ -48,7 +48,10 @@ def dgeqrdm_device(a, jpvt, tau, nb: int = 64, delta: float = 0.9, tau_: float =
     float64 tensor holding the matrix column-major (e.g. ``X.t().contiguous()``
     of a row-major m x n X has shape (n, m)); pass m, n via ``a.shape[::-1]``.
     jpvt: int32 CUDA tensor (n), tau: float64 CUDA tensor (min(m, n))."""
+    import torch
+
     n, m = a.shape
+    lib().qrdm_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream))
     nc = np.zeros(n, np.int32) if ncols is None else ncols
     nc[0] = stop
     thres = np.array([delta, tau_, 0.0 if eta is None else eta], np.float64)
@@ -100,14 +103,17 @@ class BatchedDMQR:
         self.a.copy_(torch.from_numpy(self.pack(mats)))
 
     def run(self, nb: int = 32, delta: float = 0.9, tau_: float = 0.15, stop: int = 0,
-            eta: float | None = None) -> int:
+            eta: float | None = None, precision: str = "fp64") -> int:
+        import torch
+
         thres = np.array([delta, tau_, 0.0 if eta is None else eta], np.float64)
+        lib().qrdm_set_stream(C.c_void_p(torch.cuda.current_stream().cuda_stream))
         return int(lib().dgeqrdm_batched_dev(
             self.count, self.m.ctypes.data_as(C.POINTER(C.c_int)),
             self.n.ctypes.data_as(C.POINTER(C.c_int)), C.c_void_p(self.a.data_ptr()),
             C.c_void_p(self.jpvt.data_ptr()), C.c_void_p(self.tau.data_ptr()),
             C.c_void_p(self.ncols.data_ptr()), C.c_void_p(self.info.data_ptr()),
-            thres.ctypes.data_as(C.POINTER(C.c_double)), int(stop), int(nb)))
+            thres.ctypes.data_as(C.POINTER(C.c_double)), int(stop), int(nb), PREC[precision]))
 
     def results(self) -> list:
         a = self.a.cpu().numpy()
@@ -130,13 +136,13 @@ class BatchedDMQR:
 
 
 def dgeqrdm_batched(mats, nb: int = 32, delta: float = 0.9, tau_: float = 0.15, stop: int = 0,
-                    eta: float | None = None) -> list:
+                    eta: float | None = None, precision: str = "fp64") -> list:
     """Factor a list of host matrices (uneven shapes, n <= 1024) with one
     batched DM-QR launch; returns one result dict per matrix."""
     mats = [np.asarray(A, np.float64) for A in mats]
     b = BatchedDMQR([A.shape for A in mats])
     b.load(mats)
-    r = b.run(nb=nb, delta=delta, tau_=tau_, stop=stop, eta=eta)
+    r = b.run(nb=nb, delta=delta, tau_=tau_, stop=stop, eta=eta, precision=precision)
     if r != 0:
         raise RuntimeError(f"dgeqrdm_batched_dev failed: {r}")
     return b.results()

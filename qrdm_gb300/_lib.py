@@ -44,7 +44,7 @@ SIGNATURES = {
     "dgeqrdm_dev_noalloc": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int,
                                       C.c_void_p, C.c_void_p, _pi, _pd, C.c_int, C.c_void_p]),
     "dgeqrdm_batched_dev": (C.c_int, [C.c_int, _pi, _pi, C.c_void_p, C.c_void_p, C.c_void_p,
-                                      C.c_void_p, C.c_void_p, _pd, C.c_int, C.c_int]),
+                                      C.c_void_p, C.c_void_p, _pd, C.c_int, C.c_int, C.c_int]),
     "qrdm_batched_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     "qrdm_panel_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     "dgeqp3": (C.c_int, [C.c_int, C.c_int, C.c_int, _pd, C.c_int, _pi, _pd]),

@@ -1017,13 +1017,22 @@ static unsigned long long fnv1a(unsigned long long h, const void* p, size_t n) {
   return h;
 }
 
+// Wait for the batched launch and map its device error word.
+static int batched_status(Ctx* c, cudaStream_t s) {
+  int err = 0;
+  const int* d_err = reinterpret_cast<const int*>(c->b_meta.p) + c->b_err_off;
+  CK(cudaMemcpyAsync(&err, d_err, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  return err ? QRDM_ERR_TIMEOUT : 0;
+}
+
 int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int* d_jpvt, double* d_tau,
-                        int* d_ncols, int* d_info, const double* thres, int stop, int nb) {
-  if (count < 0 || !m || !n || !thres || stop < 0 || stop > 3) return -1;
+                        int* d_ncols, int* d_info, const double* thres, int stop, int nb, int precision) {
+  if (count < 0 || !m || !n || !thres || stop < 0 || stop > 3 || precision < 0 || precision > 1) return -1;
   if (count == 0) return 0;
   const double delta = thres[0], tau_ = thres[1];
   if (delta < 0.0 || delta > 1.0 || tau_ < 0.0 || tau_ > 1.0 || nb <= 0) return -1;
-  if (nb > batched_kmax()) return QRDM_ERR_UNSUPPORTED;
+  if (nb > batched_kmax() || (precision == 1 && nb > 32)) return QRDM_ERR_UNSUPPORTED;
   int nmax = 1;
   for (int i = 0; i < count; ++i) {
     if (m[i] <= 0 || n[i] <= 0) return -1;
@@ -1062,7 +1071,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   for (int i = 0; i < count; ++i) ho[i] = work[i].second;
   const size_t meta_bytes = sizeof(long long) * count + sizeof(int) * meta.size() + sizeof(int) * 4;
   const int grid = c->nsm * batched_ctas_per_sm(nb);
-  const long long wsd = batched_ws_doubles(nmax);
+  const long long wsd = batched_ws_doubles(nmax, precision);
   unsigned long long key = 1469598103934665603ull;
   key = fnv1a(key, meta.data(), sizeof(int) * meta.size());
   void* ptrs[5] = {d_a, d_jpvt, d_tau, d_ncols, d_info};
@@ -1070,13 +1079,13 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   key = fnv1a(key, thres, sizeof(double) * 3);
   key = fnv1a(key, &nb, sizeof nb);
   key = fnv1a(key, &stop, sizeof stop);
+  key = fnv1a(key, &precision, sizeof precision);
   const size_t prof_bytes = sizeof(unsigned long long) * (size_t)grid * batched_phases();
   if (c->b_graph && key == c->b_key && c->b_meta.cap >= meta_bytes && c->b_prof.cap >= prof_bytes &&
       c->b_ws.cap >= sizeof(double) * (size_t)grid * wsd) {
     // identical batch description: replay the captured launch
     CK(cudaGraphLaunch(c->b_graph, s));
-    CK(cudaStreamSynchronize(s));
-    return 0;
+    return batched_status(c, s);
   }
   CK(c->b_meta.ensure(meta_bytes));
   CK(c->b_ws.ensure(sizeof(double) * (size_t)grid * wsd));
@@ -1084,6 +1093,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   long long* d_aoff = c->b_meta.as<long long>();
   int* d_meta = reinterpret_cast<int*>(d_aoff + count);
   int* d_queue = d_meta + meta.size();
+  c->b_err_off = (int)(d_queue + 1 - reinterpret_cast<int*>(c->b_meta.p));
   CK(cudaMemcpyAsync(d_aoff, aoff.data(), sizeof(long long) * count, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(d_meta, meta.data(), sizeof(int) * meta.size(), cudaMemcpyHostToDevice, s));
   BatchLaunch L;
@@ -1107,6 +1117,9 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   L.ws = c->b_ws.as<double>();
   L.ws_stride = wsd;
   L.queue = d_queue;
+  L.err = d_queue + 1;
+  L.mixed = precision;
+  L.nmax = nmax;
   L.prof = c->b_prof.as<unsigned long long>();
   L.grid = grid;
   c->b_grid = grid;
@@ -1139,8 +1152,7 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
   } else if (launch_batched(L, s)) {
     return QRDM_ERR_CUDA;
   }
-  CK(cudaStreamSynchronize(s));
-  return 0;
+  return batched_status(c, s);
 }
 
 int qrdm_batched_phase_cycles(unsigned long long* out, int nout) {
@@ -1189,7 +1201,7 @@ int qrdm_set_stream(void* stream) {
   int r = ctx_get(&c);
   if (r) return r;
   c->user = (cudaStream_t)stream;
-  c->user_set = stream != nullptr;
+  c->user_set = true;
   return 0;
 }
 

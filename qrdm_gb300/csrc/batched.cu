@@ -15,6 +15,8 @@
 // keeps busy with 4x4 register tiles.
 #include "common.cuh"
 #include "kernels.cuh"
+#include "ozaki_digits.cuh"
+#include "tc.cuh"
 
 namespace qrdm {
 
@@ -244,6 +246,400 @@ __device__ void cta_trailing(const double* V0, double* C0, long long lda, int ml
   }
 }
 
+// ----------------------------------------------- mixed trailing update
+// Per-CTA Ozaki-split trailing update of one DM block (kc <= 32 reflectors):
+// the FP64 operands are cut into OZS balanced base-256 digits (exact in
+// BF16), digit pairs of level <= OZS + 1 are multiplied on tcgen05 with FP32
+// accumulation in TMEM, and the levels are recombined in int64, as in the
+// single-problem kernels of ozaki.cu, here serialised inside the CTA:
+//   W^T = C^T V: 128 C columns (M) x 32 reflectors (N, the V digits stacked
+//          along N) per MMA, K = 64-row blocks of C converted by all
+//          threads; levels drained every 256 rows;
+//   W2 = T^T W in FP64, sliced per C column into global digit tiles;
+//   C -= V W2: 128-row bands (V digits, M) x 32-column tiles (W2 digits,
+//          N), K = the 32 reflectors; FP64 FMA epilogue.
+// Shared memory: adig (OZS x 16 KB), bdig (OZS x 4 KB), 1024-byte aligned.
+constexpr int OZS = 7;  // digits per operand
+
+struct OzCtx {
+  unsigned char* adig;
+  unsigned char* bdig;
+  uint32_t tmem;
+  uint64_t* bar;
+  uint32_t phase;
+  int* s_e;  // 128 column scales (shared)
+  bool fail;
+};
+
+__device__ __forceinline__ void oz_wait(OzCtx& z) {
+  if (!tc::mbar_wait(z.bar, z.phase)) z.fail = true;
+  z.phase ^= 1u;
+  tc::fence_after_sync();
+}
+
+__device__ __forceinline__ double vval(const double* V0, long long lda, int mloc, int kc, int r, int a) {
+  return (a < kc && r < mloc) ? (r > a ? V0[(size_t)a * lda + r] : (r == a ? 1.0 : 0.0)) : 0.0;
+}
+
+// levels of 16 accumulator columns (col .. col + 15) of this thread's lane:
+// hi = sum_{L<=5} D_L 2^(8(5-L)) exact; mid = sum_{L>=6} D_L 2^(8(S+1-L))
+__device__ __forceinline__ void oz_levels16(uint32_t taddr, uint32_t col, long long* hi, long long* mid) {
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    hi[j] = 0;
+    mid[j] = 0;
+  }
+#pragma unroll
+  for (int L = 2; L <= OZS + 1; ++L) {
+    float v[16];
+    tc::tmem_ld16(taddr + (uint32_t)((L - 2) * 32) + col, v);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const long long x = (long long)f32_to_int(v[j]);
+      if (L <= 5) hi[j] += x << (8 * (5 - L));
+      else mid[j] += x << (8 * (OZS + 1 - L));
+    }
+  }
+}
+
+// digit-pair MMAs of one operand pair: A digits p at a + (p-1) 16 KB, B
+// digits stacked at b (4 KB each, 32 rows), K16 steps [0, nkk); level
+// L = p + q at TMEM column (L - 2) * 32 of d
+__device__ __forceinline__ void oz_mma_block(uint32_t d, uint32_t a, uint32_t b, int nkk, bool first) {
+#pragma unroll
+  for (int p = 1; p <= OZS; ++p) {
+    const uint32_t idesc = tc::idesc_bf16_f32(128, 32 * (OZS + 1 - p));
+    for (int kk = 0; kk < nkk; ++kk)
+      tc::mma_bf16(d + (uint32_t)((p - 1) * 32), tc::desc_sw128(a + (uint32_t)(p - 1) * 16384u + kk * 32),
+                   tc::desc_sw128(b + kk * 32), idesc, (first && p == 1 && kk == 0) ? 0u : 1u);
+  }
+}
+
+// BF16 cosine Gram of the nc <= 32 scaled candidates on tcgen05 (FP32
+// accumulation in TMEM columns 0..31; candidate rows 32..127 of the A tile
+// stay zero), then an exact FP64 recheck of every cosine within `margin` of
+// delta, so each greedy decision that BF16 rounding could flip is taken on
+// an FP64 value.  Result: g (row stride gs), both triangles.
+template <class F>
+__device__ void cta_gram_tc(OzCtx& z, int mloc, int nc, F f, double* g, int gs, double delta, double margin) {
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const uint32_t asm_ = tc::smem_u32(z.adig), bsm = tc::smem_u32(z.bdig);
+  for (int e = tid; e < 96 * 32; e += 256)  // rows 32..127 of the A tile
+    reinterpret_cast<uint32_t*>(z.adig + 32 * 128)[e] = 0u;
+  const uint32_t idesc = tc::idesc_bf16_f32(128, 32);
+  for (int r0 = 0; r0 < mloc; r0 += 64) {
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int q = e >> 5, kp = e & 31, r = r0 + 2 * kp;
+      const float x0 = (q < nc && r < mloc) ? (float)f(r, q) : 0.f;
+      const float x1 = (q < nc && r + 1 < mloc) ? (float)f(r + 1, q) : 0.f;
+      const __nv_bfloat162 b2 = __floats2bfloat162_rn(x0, x1);
+      const uint32_t bits = *reinterpret_cast<const uint32_t*>(&b2);
+      const uint32_t off = tc::sw128_offset(q, 2 * kp);
+      *reinterpret_cast<uint32_t*>(z.adig + off) = bits;
+      *reinterpret_cast<uint32_t*>(z.bdig + off) = bits;
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      for (int kk = 0; kk < 4; ++kk)
+        tc::mma_bf16(z.tmem, tc::desc_sw128(asm_ + kk * 32), tc::desc_sw128(bsm + kk * 32), idesc,
+                     (r0 > 0 || kk > 0) ? 1u : 0u);
+      tc::mma_commit(z.bar);
+    }
+    oz_wait(z);
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  if (w == 0) {  // TMEM lanes 0..31 = candidate p
+    float v[32];
+    tc::tmem_ld16(z.tmem, v);
+    tc::tmem_ld16(z.tmem + 16u, v + 16);
+    tc::tmem_wait_ld();
+    if (lane < nc)
+      for (int q = 0; q < nc; ++q) g[lane * gs + q] = (double)v[q];
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  // FP64 recheck near delta: one warp per flagged pair
+  const int npair = nc * (nc - 1) / 2;
+  for (int t = w; t < npair; t += 8) {
+    int q = 1;
+    while (q * (q + 1) / 2 <= t) ++q;
+    const int pp = t - q * (q - 1) / 2;  // pp < q
+    const double c0 = g[pp * gs + q];
+    if (fabs(fabs(c0) - delta) < margin) {
+      double acc = 0.0;
+      for (int r = lane; r < mloc; r += 32) acc = fma(f(r, pp), f(r, q), acc);
+      acc = warp_sum(acc);
+      if (lane == 0) {
+        g[pp * gs + q] = acc;
+        g[q * gs + pp] = acc;
+      }
+    } else if (lane == 0) {
+      g[q * gs + pp] = c0;
+    }
+  }
+  __syncthreads();
+}
+
+// V^T V of the kc <= 32 reflectors (unit lower trapezoidal V, mloc rows)
+// with the Ozaki split on tcgen05 (the A operand is V^T: rows 0..31 of the
+// 128-row tile, the rest zero), levels drained every 256 rows.  Result in g
+// (row stride gs) as FP64.
+__device__ void cta_vtv_oz(OzCtx& z, const double* V0, long long lda, int mloc, int kc, double* g, int gs) {
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int quad = w & 3, ch = w >> 2;
+  const uint32_t tl = z.tmem + ((uint32_t)(32 * quad) << 16);
+  const uint32_t asm_ = tc::smem_u32(z.adig), bsm = tc::smem_u32(z.bdig);
+  constexpr int SH_V = 8 * OZS - 1;
+  for (int e = tid; e < OZS * 96 * 32; e += 256) {  // rows 32..127 of every A digit tile
+    const int p = e / (96 * 32), rest = e % (96 * 32);
+    reinterpret_cast<uint32_t*>(z.adig + p * 16384 + 32 * 128)[rest] = 0u;
+  }
+  long long acc_hi[16];
+  float acc_mid[16];
+#pragma unroll
+  for (int j = 0; j < 16; ++j) {
+    acc_hi[j] = 0;
+    acc_mid[j] = 0.f;
+  }
+  const int nblk = ceil_div(mloc, 64);
+  for (int kb = 0; kb < nblk; ++kb) {
+    const int r0 = kb * 64;
+    for (int e = tid; e < 32 * 32; e += 256) {
+      const int a = e >> 5, kp = e & 31, r = r0 + 2 * kp;
+      int d0[OZS], d1[OZS];
+      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, a), SH_V), d0);
+      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r + 1, a), SH_V), d1);
+      const uint32_t off = tc::sw128_offset(a, 2 * kp);
+#pragma unroll
+      for (int p = 0; p < OZS; ++p) {
+        const uint32_t pk = pack2_bf16(d0[p], d1[p]);
+        *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = pk;
+        *reinterpret_cast<uint32_t*>(z.bdig + p * 4096 + off) = pk;
+      }
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      oz_mma_block(z.tmem, asm_, bsm, 4, (kb & 3) == 0);
+      tc::mma_commit(z.bar);
+    }
+    oz_wait(z);
+    if ((kb & 3) == 3 || kb == nblk - 1) {
+      long long hi[16], mid[16];
+      oz_levels16(tl, (uint32_t)(16 * ch), hi, mid);
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        acc_hi[j] += hi[j];
+        acc_mid[j] += (float)mid[j];
+      }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+  }
+  // (V^T V)(c, a) = 2^2 (hi 256^-5 + mid 256^-(S+1)), c = this thread's lane row
+  const int c = 32 * quad + lane;
+  if (c < kc) {
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const int a = 16 * ch + j;
+      if (a < kc) g[c * gs + a] = fma((double)acc_hi[j], pow2d(2 - 40), (double)acc_mid[j] * pow2d(2 - 8 * (OZS + 1)));
+    }
+  }
+  __syncthreads();
+}
+
+__device__ void cta_trailing_oz(OzCtx& z, const double* V0, double* C0, long long lda, int mloc, int kc, int n2,
+                                int ldw, const double* T, int ldt, const double* nrmC, double* W,
+                                unsigned char* wdig, int* wexp) {
+  const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
+  const int quad = w & 3, ch = w >> 2;  // TMEM lane quadrant, 16-column half
+  const uint32_t tl = z.tmem + ((uint32_t)(32 * quad) << 16);
+  const uint32_t asm_ = tc::smem_u32(z.adig), bsm = tc::smem_u32(z.bdig);
+  constexpr int SH_V = 8 * OZS - 1;  // V scale 2^1
+  // ---------------- W^T = C^T V, 128 C columns at a time
+  const int nblk = ceil_div(mloc, 64);
+  for (int ct = 0; ct < n2; ct += 128) {
+    if (tid < 128) z.s_e[tid] = ct + tid < n2 ? scale_exp_of(nrmC[ct + tid]) : 0;
+    __syncthreads();
+    long long acc_hi[16];
+    float acc_mid[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      acc_hi[j] = 0;
+      acc_mid[j] = 0.f;
+    }
+    for (int kb = 0; kb < nblk; ++kb) {
+      const int r0 = kb * 64;
+      // C rows r0..r0+63 x 128 columns -> A digits (tile row = C column)
+      for (int it = 0; it < 16; ++it) {
+        const int e = tid + 256 * it;
+        const int rp = e & 31, cc = e >> 5;
+        const int c = ct + cc, r = r0 + 2 * rp;
+        double x0 = 0.0, x1 = 0.0;
+        if (c < n2) {
+          const double* col = C0 + (size_t)c * lda;
+          if (r < mloc) x0 = col[r];
+          if (r + 1 < mloc) x1 = col[r + 1];
+        }
+        const int sh = 8 * OZS - z.s_e[cc];
+        int d0[OZS], d1[OZS];
+        balanced_digits<OZS>(fixed_point(x0, sh), d0);
+        balanced_digits<OZS>(fixed_point(x1, sh), d1);
+        const uint32_t off = tc::sw128_offset(cc, 2 * rp);
+#pragma unroll
+        for (int p = 0; p < OZS; ++p)
+          *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+      }
+      // V rows r0..r0+63 x 32 reflectors -> B digits (tile row = reflector)
+      for (int e = tid; e < 32 * 32; e += 256) {
+        const int a = e >> 5, kp = e & 31, r = r0 + 2 * kp;
+        int d0[OZS], d1[OZS];
+        balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, a), SH_V), d0);
+        balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r + 1, a), SH_V), d1);
+        const uint32_t off = tc::sw128_offset(a, 2 * kp);
+#pragma unroll
+        for (int p = 0; p < OZS; ++p)
+          *reinterpret_cast<uint32_t*>(z.bdig + p * 4096 + off) = pack2_bf16(d0[p], d1[p]);
+      }
+      tc::fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        oz_mma_block(z.tmem, asm_, bsm, 4, (kb & 3) == 0);
+        tc::mma_commit(z.bar);
+      }
+      oz_wait(z);
+      if ((kb & 3) == 3 || kb == nblk - 1) {
+        long long hi[16], mid[16];
+        oz_levels16(tl, (uint32_t)(16 * ch), hi, mid);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          acc_hi[j] += hi[j];
+          acc_mid[j] += (float)mid[j];
+        }
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+    // W(a, c) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1)) for this thread's column
+    const int row = 32 * quad + lane, c = ct + row;
+    if (c < n2) {
+      const int e = z.s_e[row];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int a = 16 * ch + j;
+        if (a < kc)
+          W[(size_t)a * ldw + c] =
+              fma((double)acc_hi[j], pow2d(e + 1 - 40), (double)acc_mid[j] * pow2d(e + 1 - 8 * (OZS + 1)));
+      }
+    }
+    __syncthreads();
+  }
+  // ---------------- W2 = T^T W (FP64, in place in W: reflector a depends on
+  // rows b <= a only, so descending a reads unmodified rows), its column
+  // scales and digit tiles
+  for (int c = tid; c < n2; c += 256) {
+    double wv[32];
+#pragma unroll
+    for (int b = 0; b < 32; ++b) wv[b] = b < kc ? W[(size_t)b * ldw + c] : 0.0;
+    double mx = 0.0;
+#pragma unroll
+    for (int a = 31; a >= 0; --a) {
+      if (a < kc) {
+        double acc = 0.0;
+#pragma unroll
+        for (int b = 0; b <= a; ++b) acc = fma(T[a * ldt + b], wv[b], acc);
+        W[(size_t)a * ldw + c] = acc;
+        mx = fmax(mx, fabs(acc));
+      }
+    }
+    const int ew = scale_exp_of(mx);
+    wexp[c] = ew;
+    const int sh = 8 * OZS - ew;
+    unsigned char* tile = wdig + (size_t)(c >> 5) * OZS * 4096;
+    for (int ap = 0; ap < 16; ++ap) {
+      const double y0 = 2 * ap < kc ? W[(size_t)(2 * ap) * ldw + c] : 0.0;
+      const double y1 = 2 * ap + 1 < kc ? W[(size_t)(2 * ap + 1) * ldw + c] : 0.0;
+      int d0[OZS], d1[OZS];
+      balanced_digits<OZS>(fixed_point(y0, sh), d0);
+      balanced_digits<OZS>(fixed_point(y1, sh), d1);
+      const uint32_t off = tc::sw128_offset(c & 31, 2 * ap);
+#pragma unroll
+      for (int q = 0; q < OZS; ++q) *reinterpret_cast<uint32_t*>(tile + q * 4096 + off) = pack2_bf16(d0[q], d1[q]);
+    }
+  }
+  __syncthreads();
+  // ---------------- C -= V W2, 128-row bands x 32-column tiles
+  const int ntile = ceil_div(n2, 32);
+  for (int r0 = 0; r0 < mloc; r0 += 128) {
+    // V rows r0..r0+127 x 32 reflectors -> A digits (tile row = C row)
+    for (int e = tid; e < 128 * 16; e += 256) {
+      const int rr = e >> 4, ap = e & 15, r = r0 + rr;
+      int d0[OZS], d1[OZS];
+      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, 2 * ap), SH_V), d0);
+      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, 2 * ap + 1), SH_V), d1);
+      const uint32_t off = tc::sw128_offset(rr, 2 * ap);
+#pragma unroll
+      for (int p = 0; p < OZS; ++p)
+        *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+    }
+    for (int t = 0; t < ntile; ++t) {
+      {
+        const uint4* src = reinterpret_cast<const uint4*>(wdig + (size_t)t * OZS * 4096);
+        uint4* dst = reinterpret_cast<uint4*>(z.bdig);
+        uint4 v[7];
+#pragma unroll
+        for (int u = 0; u < 7; ++u) {
+          const int e = tid + 256 * u;
+          v[u] = e < OZS * 256 ? __ldcg(src + e) : make_uint4(0, 0, 0, 0);
+        }
+#pragma unroll
+        for (int u = 0; u < 7; ++u) {
+          const int e = tid + 256 * u;
+          if (e < OZS * 256) dst[e] = v[u];
+        }
+      }
+      tc::fence_async_smem();
+      __syncthreads();
+      if (tid == 0) {
+        tc::fence_after_sync();
+        oz_mma_block(z.tmem + 256u, asm_, bsm, 2, true);
+        tc::mma_commit(z.bar);
+      }
+      const int r = r0 + 32 * quad + lane;
+      const int cw0 = t * 32 + 16 * ch;
+      double cv[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const int c = cw0 + j;
+        cv[j] = (r < mloc && c < n2) ? C0[(size_t)c * lda + r] : 0.0;
+      }
+      oz_wait(z);
+      long long hi[16], mid[16];
+      oz_levels16(tl + 256u, (uint32_t)(16 * ch), hi, mid);
+      if (r < mloc && !z.fail) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int c = cw0 + j;
+          if (c < n2) {
+            const int e = 1 + wexp[c];  // V scale 2^1 times the W2 column scale
+            constexpr int msh = 8 * (OZS + 1) - 40 - 17;
+            const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
+            C0[(size_t)c * lda + r] = fma(-(double)comb, pow2d(e - 57), cv[j]);
+          }
+        }
+      }
+      tc::fence_before_sync();
+      __syncthreads();
+    }
+  }
+}
+
 struct BatchArgs {
   const int* m;
   const int* n;
@@ -263,6 +659,9 @@ struct BatchArgs {
   long long ws_stride;
   int* queue;
   unsigned long long* prof;  // per-CTA phase cycles [grid][8] or null
+  int mixed;                 // 1: trailing update on the tensor cores (Ozaki split)
+  int* err;                  // device error word (QRDM_EDEV_*)
+  int nmax;                  // largest n of the batch (workspace layout)
 };
 
 // Per-phase cycle accounting (thread 0, after the CTA barrier that ends a
@@ -278,9 +677,16 @@ constexpr int kPhases = 8;
     }                                            \
   } while (0)
 
+// Per-CTA workspace (doubles): nrm [BNMAX], nrm_exact [BNMAX], W [64][nmax],
+// then (mixed) the W2 column exponents and the W2 digit tiles.
+__host__ __device__ __forceinline__ long long ws_wexp_off(int nmax) { return 2LL * BNMAX + 64LL * nmax; }
+__host__ __device__ __forceinline__ long long ws_wdig_off(int nmax) {
+  return ws_wexp_off(nmax) + ((nmax / 2 + 2 + 1) & ~1LL);
+}
+
 template <int KB>
 __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double* ws,
-                          unsigned long long* pacc) {
+                          unsigned long long* pacc, OzCtx* oz, int nmax) {
   constexpr int GS = KB + 1;
   const int m = a.m[p], n = a.n[p];
   double* A = a.A + a.a_off[p];
@@ -371,7 +777,10 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
       auto f = [&](int r, int q) -> double {
         return q < nc ? S.tw[q] * W0[(size_t)S.cand[q].idx * lda + r] : 0.0;
       };
-      cta_gram_any<KB>(nc, mloc, f, S.stage, S.g);
+      if (KB == 32 && oz != nullptr)
+        cta_gram_tc(*oz, mloc, nc, f, S.g, GS, a.delta, 0.0078125);
+      else
+        cta_gram_any<KB>(nc, mloc, f, S.stage, S.g);
     }
     // ---- greedy pick (warp 0) and permute_marked replay (thread 0)
     const int nwords = (nloc + 31) >> 5;
@@ -564,7 +973,10 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
       auto fv = [&](int r, int q) -> double {
         return q < kc ? (r > q ? W0[(size_t)q * lda + r] : (r == q ? 1.0 : 0.0)) : 0.0;
       };
-      cta_gram_any<KB>(kc, mloc, fv, S.stage, S.g);
+      if (KB == 32 && oz != nullptr)
+        cta_vtv_oz(*oz, W0, lda, mloc, kc, S.g, GS);
+      else
+        cta_gram_any<KB>(kc, mloc, fv, S.stage, S.g);
     }
     for (int e = tid; e < KB * KB; e += blockDim.x) S.T[e] = 0.0;
     __syncthreads();
@@ -589,7 +1001,11 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
     // ---- trailing update C <- (I - V T V^T)^T C, C = window columns fjb..
     const int n2 = nloc - fjb;
     if (kc > 0 && n2 > 0) {
-      if (KB == 32 || kc <= 32)
+      if (KB == 32 && oz != nullptr)
+        cta_trailing_oz(*oz, W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, KB, nrm + j + fjb, W,
+                        reinterpret_cast<unsigned char*>(ws + ws_wdig_off(nmax)),
+                        reinterpret_cast<int*>(ws + ws_wexp_off(nmax)));
+      else if (KB == 32 || kc <= 32)
         cta_trailing<32>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, KB, S.stage, W);
       else
         cta_trailing<64>(W0, W0 + (size_t)fjb * lda, lda, mloc, kc, n2, n, S.T, KB, S.stage, W);
@@ -660,11 +1076,36 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
 // KB = 32: blocks of at most 32 columns (smem ~85 KB, <= 128 registers);
 // KB = 64: blocks of up to 64 columns.
 template <int KB>
-__global__ void __launch_bounds__(BT, KB == 32 ? 2 : 1) k_dmqr_batched(BatchArgs a) {
+__global__ void __launch_bounds__(BT, 1) k_dmqr_batched(BatchArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   BatchShared<KB>& S = *reinterpret_cast<BatchShared<KB>*>(smem_raw);
+  __shared__ uint64_t s_oz_bar;
+  __shared__ uint32_t s_oz_tmem;
+  __shared__ int s_oz_e[128];
   double* ws = a.ws + (size_t)blockIdx.x * a.ws_stride;
   const int tid = threadIdx.x;
+  // mixed: TMEM (one CTA per SM holds all 512 columns) and the digit tiles
+  // after the block's shared state, 1024-byte aligned
+  const bool mixed = KB == 32 && a.mixed;
+  OzCtx z;
+  if (mixed) {
+    uintptr_t dig = ((uintptr_t)(smem_raw + sizeof(BatchShared<KB>)) + 1023) & ~(uintptr_t)1023;
+    z.adig = reinterpret_cast<unsigned char*>(dig);
+    z.bdig = z.adig + OZS * 16384;
+    z.bar = &s_oz_bar;
+    z.phase = 0;
+    z.s_e = s_oz_e;
+    z.fail = false;
+    if (tid == 0) {
+      tc::mbar_init(&s_oz_bar, 1);
+      tc::fence_mbar_init();
+    }
+    if (tid < 32) tc::tmem_alloc(&s_oz_tmem, 512);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    z.tmem = s_oz_tmem;
+  }
   unsigned long long pacc[kPhases] = {0, 0, 0, 0, 0, 0, 0, 0};
   const long long t0 = clock64();
   pacc[7] = (unsigned long long)t0;
@@ -675,8 +1116,14 @@ __global__ void __launch_bounds__(BT, KB == 32 ? 2 : 1) k_dmqr_batched(BatchArgs
     __syncthreads();
     BPH(6);
     if (q >= a.count) break;
-    solve_one<KB>(a, a.order[q], S, ws, pacc);
+    solve_one<KB>(a, a.order[q], S, ws, pacc, mixed ? &z : nullptr, a.nmax);
     __syncthreads();
+  }
+  if (mixed) {
+    if (z.fail) atomicOr(a.err, QRDM_EDEV_BARRIER_TIMEOUT);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (tid < 32) tc::tmem_dealloc(z.tmem, 512);
   }
   if (a.prof && tid == 0) {
     for (int k = 0; k < 7; ++k) a.prof[(size_t)blockIdx.x * kPhases + k] = pacc[k];
@@ -684,18 +1131,25 @@ __global__ void __launch_bounds__(BT, KB == 32 ? 2 : 1) k_dmqr_batched(BatchArgs
   }
 }
 
-size_t batched_smem_bytes(int nb) { return nb <= 32 ? sizeof(BatchShared<32>) : sizeof(BatchShared<64>); }
+size_t batched_smem_bytes(int nb, int mixed) {
+  if (nb > 32) return sizeof(BatchShared<64>);
+  return sizeof(BatchShared<32>) + (mixed ? 1024 + (size_t)OZS * (16384 + 4096) : 0);
+}
 // One CTA per SM for both widths: two CTAs sharing an SM's FP64 pipe
 // lengthen the largest problems (which start first) and so the makespan.
 int batched_ctas_per_sm(int) { return 1; }
 int batched_phases() { return kPhases; }
 int batched_nmax() { return BNMAX; }
 int batched_kmax() { return BKMAX; }
-long long batched_ws_doubles(int nmax) { return 2LL * BNMAX + 64LL * nmax; }
+long long batched_ws_doubles(int nmax, int mixed) {
+  long long d = ws_wdig_off(nmax);
+  if (mixed) d += (long long)OZS * ((nmax + 31) / 32) * 512;
+  return (d + 1) & ~1LL;  // 16-byte multiple
+}
 
 int batched_set_attributes() {
   if (cudaFuncSetAttribute(k_dmqr_batched<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sizeof(BatchShared<32>)) != cudaSuccess)
+                           (int)batched_smem_bytes(32, 1)) != cudaSuccess)
     return 1;
   return cudaFuncSetAttribute(k_dmqr_batched<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)sizeof(BatchShared<64>)) == cudaSuccess ? 0 : 1;
@@ -725,9 +1179,12 @@ int launch_batched(const BatchLaunch& L, cudaStream_t s) {
   a.ws_stride = L.ws_stride;
   a.queue = L.queue;
   a.prof = L.prof;
-  if (cudaMemsetAsync(L.queue, 0, sizeof(int), s) != cudaSuccess) return 1;
-  if (L.nb <= 32) k_dmqr_batched<32><<<L.grid, BT, sizeof(BatchShared<32>), s>>>(a);
-  else k_dmqr_batched<64><<<L.grid, BT, sizeof(BatchShared<64>), s>>>(a);
+  a.mixed = L.mixed;
+  a.err = L.err;
+  a.nmax = L.nmax;
+  if (cudaMemsetAsync(L.queue, 0, 2 * sizeof(int), s) != cudaSuccess) return 1;  // queue, err
+  if (L.nb <= 32) k_dmqr_batched<32><<<L.grid, BT, batched_smem_bytes(32, L.mixed), s>>>(a);
+  else k_dmqr_batched<64><<<L.grid, BT, batched_smem_bytes(64, 0), s>>>(a);
   return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 

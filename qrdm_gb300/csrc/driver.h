@@ -56,11 +56,15 @@ struct Ctx {
   Buf pan_prof;                                 // clustered panel phase cycles (timing runs)
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch
   int b_grid = 0;                               // CTAs of the last batched launch
+  int b_err_off = 0;                            // int offset of its error word in b_meta
   unsigned long long b_key = 0;
   BlockState* h_st = nullptr;              // pinned host copy of the block record
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ph[8] = {};
-  cudaStream_t stream() const { return user_set ? user : own; }
+  // the caller's stream (qrdm_set_stream); NULL = the legacy default stream,
+  // which orders the library's work with every blocking stream of the
+  // caller.  `own` is used only to record CUDA graphs.
+  cudaStream_t stream() const { return user; }
 };
 
 

@@ -118,18 +118,21 @@ struct BatchLaunch {
   int nb, stop;
   double* ws;
   long long ws_stride;
-  int* queue;
+  int* queue;  // queue[0] = next problem, queue[1] = error word
   unsigned long long* prof;
   int grid;
+  int mixed;
+  int* err;
+  int nmax;
 };
 int batched_set_attributes();
 int batched_phases();
 int launch_batched(const BatchLaunch& L, cudaStream_t s);
-size_t batched_smem_bytes(int nb);
+size_t batched_smem_bytes(int nb, int mixed);
 int batched_ctas_per_sm(int nb);
 int batched_nmax();
 int batched_kmax();
-long long batched_ws_doubles(int nmax);
+long long batched_ws_doubles(int nmax, int mixed);
 
 // qp3.cu
 struct Qp3State;

@@ -30,26 +30,27 @@ def _mixed_batch():
 
 
 @pytest.mark.gpu
-def test_batched_uneven_vs_oracle(gpu_lib, oracle):
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batched_uneven_vs_oracle(gpu_lib, oracle, precision):
     import qrdm_gb300
 
     mats = _mixed_batch()
-    out = qrdm_gb300.dgeqrdm_batched(mats, nb=32, delta=0.9, tau_=0.15)
+    out = qrdm_gb300.dgeqrdm_batched(mats, nb=32, delta=0.9, tau_=0.15, precision=precision)
     assert len(out) == len(mats)
     for i, A0 in enumerate(mats):
         prefix, ref = separated(oracle, A0, P)
-        check_against(A0, out[i], ref, prefix, f"batched[{i}] {A0.shape}")
+        check_against(A0, out[i], ref, prefix, f"batched[{i}] {A0.shape} {precision}")
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nb", [8, 64])
-def test_batched_block_sizes(gpu_lib, oracle, nb):
+@pytest.mark.parametrize("nb,precision", [(8, "fp64"), (64, "fp64"), (8, "mixed"), (16, "mixed")])
+def test_batched_block_sizes(gpu_lib, oracle, nb, precision):
     import qrdm_gb300
     from qrdm_gb300.workloads import batched_matrix
 
-    shapes = [(300, 200), (128, 128), (513, 257), (65, 65), (90, 33)]
+    shapes = [(300, 200), (128, 128), (513, 257), (65, 65), (90, 33), (1100, 700)]
     mats = [batched_matrix(i, m, n, seed=21) for i, (m, n) in enumerate(shapes)]
-    out = qrdm_gb300.dgeqrdm_batched(mats, nb=nb, delta=0.5, tau_=0.3)
+    out = qrdm_gb300.dgeqrdm_batched(mats, nb=nb, delta=0.5, tau_=0.3, precision=precision)
     p = (0.5, 0.3, nb, 0, None)
     for i, A0 in enumerate(mats):
         prefix, ref = separated(oracle, A0, p)
@@ -57,13 +58,15 @@ def test_batched_block_sizes(gpu_lib, oracle, nb):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("stop,eta", [(1, None), (2, None), (3, 1e-6)])
-def test_batched_stop_modes(gpu_lib, oracle, stop, eta):
+@pytest.mark.parametrize("stop,eta,precision", [(1, None, "fp64"), (2, None, "fp64"), (3, 1e-6, "fp64"),
+                                                (1, None, "mixed")])
+def test_batched_stop_modes(gpu_lib, oracle, stop, eta, precision):
     import qrdm_gb300
     from qrdm_gb300.workloads import rank_deficient_demo
 
     mats = [rank_deficient_demo(96, seed=s) for s in range(4)]
-    out = qrdm_gb300.dgeqrdm_batched(mats, nb=16, delta=0.9, tau_=0.15, stop=stop, eta=eta)
+    out = qrdm_gb300.dgeqrdm_batched(mats, nb=16, delta=0.9, tau_=0.15, stop=stop, eta=eta,
+                                     precision=precision)
     p = (0.9, 0.15, 16, stop, eta)
     for i, A0 in enumerate(mats):
         prefix, ref = separated(oracle, A0, p)
@@ -82,14 +85,14 @@ def test_batched_graph_replay(gpu_lib, oracle):
 
     shapes = [(200, 150), (64, 64), (400, 100), (33, 17)]
     b = BatchedDMQR(shapes)
-    for seed in (31, 32, 33):
+    for seed, prec in ((31, "fp64"), (32, "fp64"), (33, "mixed"), (34, "mixed")):
         mats = [batched_matrix(i, m, n, seed=seed) for i, (m, n) in enumerate(shapes)]
         b.load(mats)
-        assert b.run(nb=32) == 0
+        assert b.run(nb=32, precision=prec) == 0
         out = b.results()
         for i, A0 in enumerate(mats):
             prefix, ref = separated(oracle, A0, P)
-            check_against(A0, out[i], ref, prefix, f"replay seed={seed} [{i}]")
+            check_against(A0, out[i], ref, prefix, f"replay seed={seed} {prec} [{i}]")
 
 
 @pytest.mark.gpu
@@ -114,13 +117,15 @@ def test_batched_argument_errors(gpu_lib):
 
     b = BatchedDMQR([(8, 8)])
     assert b.run(nb=65) == 1003          # nb beyond the batched kernel
+    assert b.run(nb=64, precision="mixed") == 1003  # mixed: nb <= 32
     assert b.run(nb=0) == -1
     assert b.run(nb=8, delta=1.5) == -1
     assert b.run(nb=8, stop=4) == -1
     big = BatchedDMQR([(4, 1025)])
     assert big.run(nb=8) == 1003         # n beyond the batched kernel
     thres = (C.c_double * 3)(0.9, 0.15, 0.0)
-    assert gpu_lib.dgeqrdm_batched_dev(0, None, None, None, None, None, None, None, thres, 0, 8) == -1
+    assert gpu_lib.dgeqrdm_batched_dev(0, None, None, None, None, None, None, None, thres, 0, 8, 0) == -1
     m = (C.c_int * 1)(0)
     n = (C.c_int * 1)(4)
-    assert gpu_lib.dgeqrdm_batched_dev(1, m, n, None, None, None, None, None, thres, 0, 8) == -1
+    assert gpu_lib.dgeqrdm_batched_dev(1, m, n, None, None, None, None, None, thres, 0, 8, 0) == -1
+    assert gpu_lib.dgeqrdm_batched_dev(1, m, n, None, None, None, None, None, thres, 0, 8, 2) == -1
