@@ -527,7 +527,7 @@ def batched_errors(b, pristine):
     return np.array(be), np.array(orth)
 
 
-def batched_cpu_sample(b_shapes, pristine_host, offs, threads, seed=7):
+def batched_cpu_sample(b_shapes, pristine_host, offs, threads, seed=7, nb=BATCH_NB):
     """Oracle DM-QR over a seeded random sample of the batch's problems."""
     from oracle.oracle import Oracle, run_dmqr
 
@@ -540,7 +540,7 @@ def batched_cpu_sample(b_shapes, pristine_host, offs, threads, seed=7):
         mats.append(pristine_host[offs[i]:offs[i + 1]].reshape(n, m).T)
     t0 = time.perf_counter()
     for A0 in mats:
-        r = run_dmqr(o, A0, nb=BATCH_NB, delta=DELTA, tau_=TAU_)
+        r = run_dmqr(o, A0, nb=nb, delta=DELTA, tau_=TAU_)
         assert r["info"] == 0
     dt = time.perf_counter() - t0
     return {"value": len(mats) / dt, "seconds": dt, "problems": len(mats)}
@@ -560,10 +560,20 @@ def run_batched(args):
     count = len(shapes)
     pristine = b.a.clone()
     launches_per_step = 1
+    tuned = None
+    if args.batch_nb > 0:
+        bnb, bprec = args.batch_nb, args.precision
+    else:
+        # block size and arithmetic from the autotuner (timed on a sample of
+        # the batch's shapes)
+        from qrdm_gb300.autotune import tune_batched
+
+        tuned = tune_batched(shapes, delta=DELTA, tau_=TAU_)
+        bnb, bprec = tuned["nb"], tuned["precision"]
 
     def step():
         b.a.copy_(pristine)
-        r = b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_, precision=args.precision)
+        r = b.run(nb=bnb, delta=DELTA, tau_=TAU_, precision=bprec)
         if r != 0:
             raise RuntimeError(f"dgeqrdm_batched_dev returned {r}")
 
@@ -594,7 +604,7 @@ def run_batched(args):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_, precision=args.precision)
+        b.run(nb=bnb, delta=DELTA, tau_=TAU_, precision=bprec)
         e1.record(stream)
         torch.cuda.synchronize()
         kms = e0.elapsed_time(e1)
@@ -611,7 +621,7 @@ def run_batched(args):
             be, orth = np.full(1, np.nan), np.full(1, np.nan)
         achieved = F / (kms / 1e3) / 1e12
         roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch; trailing update "
-                "on " + ("BF16 tensor cores, Ozaki split" if args.precision == "mixed" else "FP64") + ")",
+                "on " + ("BF16 tensor cores, Ozaki split" if bprec == "mixed" else "FP64") + ")",
                 "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
                 "peak_kind": "nominal FP64 (no measured FP64 peak); HBM term from measured "
                              f"{peaks['hbm_gbs']} GB/s", "unit": "TFLOP/s",
@@ -628,7 +638,7 @@ def run_batched(args):
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             b.a.copy_(host, non_blocking=True)
-            b.run(nb=BATCH_NB, delta=DELTA, tau_=TAU_, precision=args.precision)
+            b.run(nb=bnb, delta=DELTA, tau_=TAU_, precision=bprec)
             back.copy_(b.a, non_blocking=True)
             jp_h = b.jpvt.cpu()
             tau_h = b.tau.cpu()
@@ -641,7 +651,7 @@ def run_batched(args):
         cpu = None
         if args.cpu_baseline:
             threads = os.cpu_count() or 1
-            s = batched_cpu_sample(shapes, pristine.cpu().numpy(), b.a_off, threads)
+            s = batched_cpu_sample(shapes, pristine.cpu().numpy(), b.a_off, threads, nb=bnb)
             cpu = {"value": s["value"], "unit": "matrices/s", "cores": threads, "kind": "port",
                    "sample": f"{s['problems']} problems of the batch drawn by seed, factored one "
                              f"after another by the oracle port on OpenBLAS ({s['seconds']:.1f} s)"}
@@ -649,8 +659,8 @@ def run_batched(args):
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic",
-               "config": {"workload": "batched2000", "count": count, "nb": BATCH_NB,
-                          "precision": args.precision,
+               "config": {"workload": "batched2000", "count": count, "nb": bnb,
+                          "precision": bprec, "autotune": tuned,
                           "delta": DELTA, "tau_": TAU_, "flops": F, "generator": BATCH_GENERATOR,
                           "bytes": 8 * pristine.numel(),
                           "parallelism": f"replicas{world}",
@@ -714,6 +724,8 @@ def main():
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--count", type=int, default=None,
                     help="batched2000: number of problems (default 2000)")
+    ap.add_argument("--batch-nb", type=int, default=0,
+                    help="batched2000: DM block size (0: autotuner picks nb and precision)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     args = ap.parse_args()
     if args.workload == "batched2000":

@@ -1,0 +1,89 @@
+"""Autotuner for the batched DM-QR launch.
+
+The batched kernel has two free choices per batch: the DM block size nb
+(which also selects the kernel's shared-memory layout: nb <= 32 uses the
+compact layout that leaves room for the tensor-core tiles) and the
+arithmetic of the trailing update, Gram and V^T V (``"fp64"`` or
+``"mixed"``, the Ozaki split on the BF16 tensor cores).  The tuner times
+each candidate on the batch itself (or a seeded sample of it: the largest
+problems plus a uniform draw, which keeps the makespan structure) with CUDA
+events and keeps the fastest.  Results are cached per batch signature
+(count, and the shape distribution rounded to powers of two) for the life of
+the process.
+
+nb is a DM parameter: it changes the block boundaries and hence the pivots
+a user gets.  The tuner is therefore opt-in (``BatchedDMQR.run(nb="auto")``
+is not implied anywhere); parity tests always pass an explicit nb.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+DEFAULT_CANDIDATES = ((32, "mixed"), (16, "mixed"), (8, "mixed"), (32, "fp64"), (64, "fp64"))
+_CACHE: dict = {}
+
+
+def signature(shapes) -> tuple:
+    m = np.array([s[0] for s in shapes])
+    n = np.array([s[1] for s in shapes])
+    q = lambda a: tuple(int(2 ** round(math.log2(max(1, x)))) for x in np.percentile(a, [10, 50, 90, 100]))
+    return (len(shapes), q(m), q(n))
+
+
+def _sample(shapes, limit: int, seed: int = 0):
+    if len(shapes) <= limit:
+        return list(range(len(shapes)))
+    flops = np.array([2.0 * m * n * n for m, n in shapes])
+    order = np.argsort(-flops)
+    big = list(order[: limit // 4])
+    rest = np.setdiff1d(np.arange(len(shapes)), big)
+    rng = np.random.default_rng(seed)
+    return sorted(big + list(rng.choice(rest, size=limit - len(big), replace=False)))
+
+
+def tune_batched(shapes, mats=None, candidates=DEFAULT_CANDIDATES, sample: int | None = 600,
+                 delta: float = 0.9, tau_: float = 0.15, reps: int = 2, seed: int = 0) -> dict:
+    """Time each (nb, precision) candidate on the batch (or a sample of it)
+    and return {"nb", "precision", "ms": {candidate: ms}, "sample": count}.
+    mats: the host matrices (optional; seeded synthetic matrices of the same
+    shapes otherwise)."""
+    import torch
+
+    from . import BatchedDMQR
+    from .workloads import batched_matrix
+
+    key = (signature(shapes), tuple(candidates), sample)
+    if key in _CACHE:
+        return _CACHE[key]
+    idx = _sample(shapes, sample or len(shapes), seed)
+    sub = [shapes[i] for i in idx]
+    b = BatchedDMQR(sub)
+    if mats is not None:
+        host = b.pack([mats[i] for i in idx])
+    else:
+        host = b.pack([batched_matrix(k, m, n, seed=seed + 17) for k, (m, n) in enumerate(sub)])
+    pristine = torch.from_numpy(host).to(b.a.device)
+    stream = torch.cuda.current_stream()
+    times = {}
+    for nb, prec in candidates:
+        best = float("inf")
+        for rep in range(reps + 1):
+            b.a.copy_(pristine)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            rc = b.run(nb=nb, delta=delta, tau_=tau_, precision=prec)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            if rc != 0:
+                best = float("inf")
+                break
+            if rep > 0:  # the first run records the launch graph
+                best = min(best, e0.elapsed_time(e1))
+        times[f"nb={nb},{prec}"] = best
+    nb, prec = min(candidates, key=lambda c: times[f"nb={c[0]},{c[1]}"])
+    out = {"nb": nb, "precision": prec, "ms": times, "sample": len(sub)}
+    _CACHE[key] = out
+    return out

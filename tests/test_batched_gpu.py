@@ -129,3 +129,25 @@ def test_batched_argument_errors(gpu_lib):
     n = (C.c_int * 1)(4)
     assert gpu_lib.dgeqrdm_batched_dev(1, m, n, None, None, None, None, None, thres, 0, 8, 0) == -1
     assert gpu_lib.dgeqrdm_batched_dev(1, m, n, None, None, None, None, None, thres, 0, 8, 2) == -1
+
+
+@pytest.mark.gpu
+def test_batched_autotune(gpu_lib):
+    """The autotuner times its candidates on the batch's shapes and returns
+    one of them; the chosen configuration factors the batch correctly."""
+    import qrdm_gb300
+    from qrdm_gb300.autotune import DEFAULT_CANDIDATES, tune_batched
+    from qrdm_gb300.metrics import factor_metrics
+    from qrdm_gb300.workloads import batched_matrix, batched_shapes
+
+    ms, ns = batched_shapes(count=40, seed=13, nmin=16, nmax=160, mcap=400)
+    shapes = [(int(m), int(n)) for m, n in zip(ms, ns)]
+    t = tune_batched(shapes, sample=None, reps=1)
+    assert (t["nb"], t["precision"]) in DEFAULT_CANDIDATES
+    assert all(v < float("inf") for v in t["ms"].values()), t
+    assert tune_batched(shapes, sample=None, reps=1) is t  # cached per signature
+    mats = [batched_matrix(i, m, n, seed=13) for i, (m, n) in enumerate(shapes)]
+    out = qrdm_gb300.dgeqrdm_batched(mats, nb=t["nb"], precision=t["precision"])
+    for A0, r in zip(mats, out):
+        met = factor_metrics(A0, r["A"], r["tau"], r["jpvt"])
+        assert met["backward"] <= 10 * max(A0.shape) * 2.0 ** -53
