@@ -361,7 +361,12 @@ def run_ours(args):
                     "k_oz_gemm1, k_oz_w2, k_oz_gemm2), BF16 tcgen05", "achieved": achieved,
                     "peak": peak, "peak_kind": f"{peak_kind} bf16 sustained (the phase runs "
                     "inside a long step)", "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": load_traffic("trail_ozaki"),
+                    "traffic": (load_traffic("trail_ozaki") * sti.trail_flops / (4.0 * NB) / max(nblk, 1)
+                                if load_traffic("trail_ozaki") else None),
+                    "traffic_basis": "bytes per DM block (one launch of each of the four kernels): "
+                                     "21.8 B per C entry measured on the 4096^2 case "
+                                     "(profiles/oz_trailing_update_gauss4k.md) x the average m' n' "
+                                     "of this workload's blocks",
                     "per_launch_basis": f"{prods} BF16 digit products x 4 m' n' k flops per DM "
                                         f"block, {nblk} blocks",
                     "fp64_equivalent_tflops": (sti.trail_flops / (sti.ms_trail / 1e3) / 1e12
