@@ -164,15 +164,16 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 // over the 256-row chunks [chunk_begin, chunk_end) of the window.
 // Wp[split][c][a] (FP64).  C columns start at window column st->fjb.
 //
-// Warp-specialised pipeline per 64-row block.  Warps 0..7 convert C from
-// FP64 into its digits (the A operand), half a block (32 rows = K16 steps
-// 2h, 2h+1) at a time, into one of two half-buffers, and announce each half
-// on an mbarrier; the loads of the next half are in flight meanwhile.  Warp
-// 8 (one lane) waits for a half, issues its digit-pair MMAs and commits them
-// to that half's "free" barrier, and keeps the V digits (B operand) of the
-// next block arriving by bulk copy into the second of two buffers.  After
-// the last block of a 256-row chunk the converter warps drain the levels
-// into their integer accumulators and release the TMEM to the next chunk.
+// Warp-specialised pipeline per 64-row block.  Sixteen converter warps
+// turn C from FP64 into its digits (the A operand), half a block (32 rows =
+// K16 steps 2h, 2h+1) at a time, into one of two half-buffers, and announce
+// each half on an mbarrier; the loads of the next half are in flight
+// meanwhile.  One more warp (one lane) waits for a half, issues its
+// digit-pair MMAs and commits them to that half's "free" barrier, and keeps
+// the V digits (B operand) of the next block arriving by bulk copy into the
+// second of two buffers.  After the last block of a 256-row chunk the
+// converter warps drain the levels into their integer accumulators (16
+// reflector columns each) and release the TMEM to the next chunk.
 struct OzG1Args {
   const double* W0;     // window origin A(j, j)
   long long lda;
@@ -185,7 +186,10 @@ struct OzG1Args {
   BlockState* st;
 };
 
-constexpr int OZ_G1_THREADS = 288;  // 8 converter warps + 1 MMA warp
+constexpr int OZ_G1_CONV = 16;                         // converter warps
+constexpr int OZ_G1_THREADS = 32 * (OZ_G1_CONV + 1);  // + 1 MMA warp
+constexpr int OZ_G1_PAIRS = 2048 / (32 * OZ_G1_CONV);  // row pairs per thread per half block
+constexpr int OZ_G1_CPT = 256 / OZ_G1_CONV;            // drained reflector columns per thread
 
 template <int S>
 __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
@@ -212,12 +216,12 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   }
   if (tid == 0) {
     for (int h = 0; h < 2; ++h) {
-      tc::mbar_init(&afull[h], 8);
+      tc::mbar_init(&afull[h], OZ_G1_CONV);
       tc::mbar_init(&aempty[h], 1);
       tc::mbar_init(&bfull[h], 1);
     }
     tc::mbar_init(&dready, 1);
-    tc::mbar_init(&dfree, 8);
+    tc::mbar_init(&dfree, OZ_G1_CONV);
     tc::fence_mbar_init();
   }
   if (w == 0) tc::tmem_alloc(&s_tmem, 512);
@@ -226,7 +230,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
   bool fail = false;
-  if (w == 8) {
+  if (w == OZ_G1_CONV) {
     // ---------------- MMA issuer and V-digit producer (one lane)
     if (lane == 0 && nblk > 0) {
       tc::mbar_arrive_expect_tx(&bfull[0], BBYTES);
@@ -260,25 +264,26 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
       tc::mbar_wait(&aempty[1], (uint32_t)((nblk - 1) & 1));
     }
   } else {
-    // ---------------- converters (256 threads) and level drains
+    // ---------------- converters and level drains
     const int row = 32 * (w & 3) + lane;  // TMEM lane = tile row = C column (c0 + row)
-    const int half = w >> 2;              // reflector columns [32 half, 32 half + 32)
+    const int cgrp = w >> 2;              // reflector columns [CPT cgrp, CPT cgrp + CPT)
     const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
-    long long acc_hi[32];
-    float acc_mid[32];
+    long long acc_hi[OZ_G1_CPT];
+    float acc_mid[OZ_G1_CPT];
 #pragma unroll
-    for (int i = 0; i < 32; ++i) {
+    for (int i = 0; i < OZ_G1_CPT; ++i) {
       acc_hi[i] = 0;
       acc_mid[i] = 0.f;
     }
-    // C rows r0 + 32 h + [0, 32) x columns c0 + [0, 128): 8 row pairs per
-    // thread, 16 consecutive threads on one column (256 contiguous bytes)
-    double2 xv[8];
+    // C rows r0 + 32 h + [0, 32) x columns c0 + [0, 128): row pairs spread
+    // over the converter threads, 16 consecutive threads on one column (256
+    // contiguous bytes)
+    double2 xv[OZ_G1_PAIRS];
     auto load_half = [&](int ib, int h) {
       const int rb = (ch_begin + (ib >> 2)) * 256 + (ib & 3) * 64 + 32 * h;
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int e = tid + 256 * u;
+      for (int u = 0; u < OZ_G1_PAIRS; ++u) {
+        const int e = tid + 32 * OZ_G1_CONV * u;
         const int rp = e & 15, cc = e >> 4;
         const int c = c0 + cc, r = rb + 2 * rp;
         double2 x = make_double2(0.0, 0.0);
@@ -302,8 +307,8 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         // the MMAs that read this half for the previous block are complete
         if (ib >= 1 && !tc::mbar_wait(&aempty[h], (uint32_t)((ib - 1) & 1))) fail = true;
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int e = tid + 256 * u;
+        for (int u = 0; u < OZ_G1_PAIRS; ++u) {
+          const int e = tid + 32 * OZ_G1_CONV * u;
           const int rp = e & 15, cc = e >> 4;
           const int sh = 8 * S - s_e[cc];
           int d0[S], d1[S];
@@ -326,9 +331,9 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         if (!tc::mbar_wait(&dready, (uint32_t)((ib >> 2) & 1))) fail = true;
         tc::fence_after_sync();
 #pragma unroll
-        for (int g8 = 0; g8 < 4; ++g8) {
+        for (int g8 = 0; g8 < OZ_G1_CPT / 8; ++g8) {
           long long hi[8], mid[8];
-          oz_levels8<S>(taddr, 32 * half + 8 * g8, hi, mid);
+          oz_levels8<S>(taddr, OZ_G1_CPT * cgrp + 8 * g8, hi, mid);
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             acc_hi[8 * g8 + i] += hi[i];
@@ -347,8 +352,8 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
       if (c < g.ncols) {
         const int e = s_e[row];
 #pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          const int a = 32 * half + i;
+        for (int i = 0; i < OZ_G1_CPT; ++i) {
+          const int a = OZ_G1_CPT * cgrp + i;
           double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
           out[a] = a < k ? v : 0.0;
         }
