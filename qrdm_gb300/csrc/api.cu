@@ -229,9 +229,9 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
   k_vtv_stored<<<nchunk, 256, 0, s>>>(V, ldv, mloc, rpc, d_st, c.vtv_part.as<double>());
   RET(check_launch());
   int npair = kmax * (kmax - 1) / 2;
-  k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), nchunk, d_st, c.vtv.as<double>());
+  k_vtv_reduce<<<std::max(1, ceil_div(8 * npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), nchunk, d_st, c.vtv.as<double>());
   RET(check_launch());
-  k_larft<<<1, 32 * ceil_div(4 * kmax, 32), sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), tau, d_st, c.T.as<double>(), kmax);
+  launch_larft(c.vtv.as<double>(), tau, d_st, c.T.as<double>(), kmax, s);
   RET(check_launch());
   return 0;
 }
@@ -450,9 +450,9 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     // ---- T factor (dlarft 'F','C', src/dgeqrdm_work.c:751-754)
     {
       int npair = kmax * (kmax - 1) / 2;
-      k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
+      k_vtv_reduce<<<std::max(1, ceil_div(8 * npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
       RET(check_launch());
-      k_larft<<<1, 32 * ceil_div(4 * kmax, 32), sizeof(double) * (size_t)kmax * kmax, s>>>(c.vtv.as<double>(), P.tau + j, d_st, c.T.as<double>(), kmax);
+      launch_larft(c.vtv.as<double>(), P.tau + j, d_st, c.T.as<double>(), kmax, s);
       RET(check_launch());
     }
     PH(3);
@@ -638,8 +638,8 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
     pa.prof = nullptr;
     RET(launch_panel(c, pa, mloc, kb, s, &G));
     int npair = kb * (kb - 1) / 2;
-    k_vtv_reduce<<<std::max(1, ceil_div(npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
-    k_larft<<<1, 32 * ceil_div(4 * kb, 32), sizeof(double) * (size_t)kb * kb, s>>>(c.vtv.as<double>(), d_tau + j, d_st, c.T.as<double>(), kb);
+    k_vtv_reduce<<<std::max(1, ceil_div(8 * npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
+    launch_larft(c.vtv.as<double>(), d_tau + j, d_st, c.T.as<double>(), kb, s);
     RET(check_launch());
     double* W0 = d_a + (size_t)j * lda + j;
     RET(apply_block_reflector(c, s, W0, lda, W0 + (size_t)kb * lda, lda, mloc, n - j - kb, 0, 1, kb, d_st));

@@ -89,6 +89,8 @@ constexpr int kPanelClusterSize = 8;
 __global__ void k_vtv_reduce(const double* vtv_part, int G, const BlockState* st, double* vtv);
 __global__ void k_larft(const double* vtv, const double* tau, const BlockState* st, double* T,
                         int ldt);
+void launch_larft(const double* vtv, const double* tau, const BlockState* st, double* T, int kmax,
+                  cudaStream_t s);
 
 // trail64.cu
 void launch_trail_w_partial(int KT, dim3 grid, cudaStream_t s, const TrailArgs& a);

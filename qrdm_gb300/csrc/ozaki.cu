@@ -40,42 +40,54 @@ constexpr int OZ_TPB = 256;
 // V (mloc x k, unit lower trapezoidal, window origin V) -> digit tiles:
 //   va2[t][p]: rows 128t..128t+127, K = the 64 reflector columns (GEMM2 A)
 //   vb1[b][p]: N = the 64 reflector columns, K = rows 64b..64b+63 (GEMM1 B)
-// fixed scale 2^1.  One thread per (row, pair of reflector columns).
+// fixed scale 2^1.  One CTA per 64-row block: each thread cuts 2 x 2 entries
+// (two rows, two reflectors) into digits and packs them for both layouts in
+// shared memory (the block's vb1 tile and its half of a va2 tile are 8 KB
+// contiguous per digit), then the tiles go out as 16-byte stores.
 template <int S>
 __global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict__ V, long long ldv, int mloc,
                                                         const BlockState* __restrict__ st,
                                                         unsigned char* __restrict__ va2,
                                                         unsigned char* __restrict__ vb1) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  unsigned char* sb = smem_raw;             // S x 8 KB: vb1 tile of this block
+  unsigned char* sa = smem_raw + S * 8192;  // S x 8 KB: rows 64 (b & 1).. of va2 tile b / 2
   const int k = st->fjb_cmp;
-  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  const int mpad = ceil_div(mloc, 256) * 256;
-  if (e >= (long long)mpad * 32) return;
-  const int r = (int)(e / 32), ap = (int)(e % 32);  // row, column pair
+  const int b = blockIdx.x, r0 = 64 * b;
   const int sh = 8 * S - 1;
-  int dg[2][S];
+  for (int q = threadIdx.x; q < 32 * 32; q += blockDim.x) {
+    const int rp = q >> 5, ap = q & 31;  // rows 2rp, 2rp+1; reflectors 2ap, 2ap+1
+    int d[2][2][S];
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int a = 2 * ap + h;
-    double v = 0.0;
-    if (r < mloc && a < k) v = r > a ? V[(size_t)a * ldv + r] : (r == a ? 1.0 : 0.0);
-    balanced_digits<S>(fixed_point(v, sh), dg[h]);
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        const int r = r0 + 2 * rp + i, a = 2 * ap + h;
+        double v = 0.0;
+        if (r < mloc && a < k) v = r > a ? V[(size_t)a * ldv + r] : (r == a ? 1.0 : 0.0);
+        balanced_digits<S>(fixed_point(v, sh), d[i][h]);
+      }
+#pragma unroll
+    for (int p = 0; p < S; ++p) {
+#pragma unroll
+      for (int i = 0; i < 2; ++i)  // va2: row 2rp+i, K = reflector pair
+        *reinterpret_cast<uint32_t*>(sa + p * 8192 + tc::sw128_offset(2 * rp + i, 2 * ap)) =
+            pack2_bf16(d[i][0][p], d[i][1][p]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h)  // vb1: row = reflector, K = row pair
+        *reinterpret_cast<uint32_t*>(sb + p * 8192 + tc::sw128_offset(2 * ap + h, 2 * rp)) =
+            pack2_bf16(d[0][h][p], d[1][h][p]);
+    }
   }
-  const int t = r >> 7, rr = r & 127;
-#pragma unroll
-  for (int p = 0; p < S; ++p) {
-    // GEMM2 A tile: row rr, K = a (pair packed)
-    unsigned char* ta = va2 + ((size_t)t * S + p) * 16384;
-    *reinterpret_cast<uint32_t*>(ta + tc::sw128_offset(rr, 2 * ap)) = pack2_bf16(dg[0][p], dg[1][p]);
-  }
-  // GEMM1 B tile: row (N) = a, K = r % 64 -- the two reflector columns land in
-  // different rows; store 16-bit values
-  const int b = r >> 6, kr = r & 63;
-#pragma unroll
-  for (int p = 0; p < S; ++p) {
-    unsigned char* tb = vb1 + ((size_t)b * S + p) * 8192;
-#pragma unroll
-    for (int h = 0; h < 2; ++h)
-      *reinterpret_cast<unsigned short*>(tb + tc::sw128_offset(2 * ap + h, kr)) = bf16_bits(dg[h][p]);
+  __syncthreads();
+  uint4* gb = reinterpret_cast<uint4*>(vb1 + (size_t)b * S * 8192);
+  const uint4* lb = reinterpret_cast<const uint4*>(sb);
+  for (int e = threadIdx.x; e < S * 512; e += blockDim.x) gb[e] = lb[e];
+  const int t = b >> 1, half = b & 1;
+  for (int e = threadIdx.x; e < S * 512; e += blockDim.x) {
+    const int p = e >> 9, off = e & 511;
+    reinterpret_cast<uint4*>(va2 + ((size_t)t * S + p) * 16384 + half * 8192)[off] =
+        reinterpret_cast<const uint4*>(sa + p * 8192)[off];
   }
 }
 
@@ -624,6 +636,9 @@ size_t oz_gemm_smem(int s) { return oz_gemm1_smem(s); }
 
 template <int S>
 static int oz_set_attributes_s() {
+  if (cudaFuncSetAttribute(k_oz_slice_v<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, S * 16384) !=
+      cudaSuccess)
+    return 1;
   if (cudaFuncSetAttribute(k_oz_gemm1<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)oz_gemm1_smem(S)) !=
       cudaSuccess)
     return 1;
@@ -643,7 +658,7 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
                   const double* T, int ldt, int nsm, BlockState* st, unsigned char* va2, unsigned char* vb1,
                   unsigned char* wb2, int* wexp, double* Wp) {
   const int mpad = ceil_div(mloc, 256) * 256;
-  k_oz_slice_v<S><<<ceil_div(mpad * 32, OZ_TPB), OZ_TPB, 0, st_>>>(W0, lda, mloc, st, va2, vb1);
+  k_oz_slice_v<S><<<mpad / 64, OZ_TPB, (size_t)S * 16384, st_>>>(W0, lda, mloc, st, va2, vb1);
   const int ctiles = ceil_div(ncols - 1, 128);  // >= 1 column is selected
   const int nchunk = ceil_div(mloc, 256);
   int nsplit = std::max(1, std::min(nchunk, ceil_div(2 * nsm, ctiles)));

@@ -574,50 +574,83 @@ __global__ void __launch_bounds__(256) k_vtv_stored(const double* __restrict__ V
 // column: vtv[b(b-1)/2 + a] for a < b < k.
 __global__ void k_vtv_reduce(const double* __restrict__ vtv_part, int G,
                              const BlockState* __restrict__ st, double* __restrict__ vtv) {
+  // 8 threads per pair: each sums a contiguous eighth of the G partials in
+  // order (loads in flight ahead of the additions), then the eight sums are
+  // combined by a fixed shuffle tree (deterministic)
   const int k = st->fjb_cmp;
-  int npair = k * (k - 1) / 2;
-  int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= npair) return;
-  int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
-  while (b * (b - 1) / 2 > t) --b;
-  while ((b + 1) * b / 2 <= t) ++b;
-  int a = t - b * (b - 1) / 2;
+  const int npair = k * (k - 1) / 2;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = gt >> 3, part = gt & 7;
   double s = 0.0;
-  for (int q = 0; q < G; ++q) s += vtv_part[(size_t)q * QRDM_NB_MAX * QRDM_NB_MAX + a * QRDM_NB_MAX + b];
-  vtv[t] = s;
+  if (t < npair) {
+    int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+    while (b * (b - 1) / 2 > t) --b;
+    while ((b + 1) * b / 2 <= t) ++b;
+    const int a = t - b * (b - 1) / 2;
+    const double* src = vtv_part + a * QRDM_NB_MAX + b;
+    const size_t stride = (size_t)QRDM_NB_MAX * QRDM_NB_MAX;
+    const int q0 = (G * part) / 8, q1 = (G * (part + 1)) / 8;
+    int q = q0;
+    for (; q + 4 <= q1; q += 4) {
+      double v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = __ldcg(src + (size_t)(q + u) * stride);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) s += v[u];
+    }
+    for (; q < q1; ++q) s += __ldcg(src + (size_t)q * stride);
+  }
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  s += __shfl_xor_sync(0xffffffffu, s, 4);
+  if (t < npair && part == 0) vtv[t] = s;
 }
 
-// T factor of the block reflector H(0)..H(k-1) = I - V T V^T ('F','C'):
-// T(i,i) = tau_i; T(0:i, i) = -tau_i T(0:i,0:i) (V(:,0:i)^T v_i) (zero when
-// tau_i = 0), from the reduced V^T V.  One CTA; T is built in shared memory
-// (dynamic, kmax^2 doubles) and stored column-major with leading dim ldt.
-__global__ void __launch_bounds__(512) k_larft(const double* __restrict__ vtv,
-                                               const double* __restrict__ tau,
-                                               const BlockState* __restrict__ st,
-                                               double* __restrict__ T, int ldt) {
+// T factor of the block reflector H(0)..H(k-1) = I - V T V^T ('F','C'),
+// from the reduced V^T V.  T is the inverse of the upper triangular
+// U = diag(1/tau) + strict_upper(V^T V) (the compact-WY identity of
+// Schreiber & Van Loan), so each column j of T is an independent
+// back-substitution: T(j,j) = tau_j and, for i = j-1 .. 0,
+// T(i,j) = -tau_i sum_{l=i+1..j} U(i,l) T(l,j) (row i zero when tau_i = 0,
+// as in dlarft).  One warp (one CTA) per column, the sum over l spread over
+// the lanes: the columns run on as many SMs as there are columns, and each
+// column's serial chain of j steps costs a few FP64 warp instructions per
+// step (a single warp reaches only a quarter of an SM's FP64 rate, so the
+// chain, not the flops, bounds the kernel).  V^T V is staged in shared
+// memory first (coalesced), since every step reads scattered entries.
+__global__ void __launch_bounds__(32) k_larft(const double* __restrict__ vtv,
+                                              const double* __restrict__ tau,
+                                              const BlockState* __restrict__ st,
+                                              double* __restrict__ T, int ldt) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  double* sT = reinterpret_cast<double*>(smem_raw);  // [k][k] column-major
-  __shared__ double s_y[QRDM_NB_MAX];
   const int k = st->fjb_cmp;
-  for (int e = threadIdx.x; e < k * k; e += blockDim.x) sT[e] = 0.0;
-  __syncthreads();
-  // column i: T(a, i) = sum_{b=a}^{i-1} T(a, b) y_b, y = -tau_i V^T v_i;
-  // 4 threads per output row a (interleaved b), combined by shuffles
-  const int a = threadIdx.x >> 2, part = threadIdx.x & 3;
-  for (int i = 0; i < k; ++i) {
+  const int j = blockIdx.x;
+  if (j >= k) return;
+  double* sU = reinterpret_cast<double*>(smem_raw);  // packed strict upper, U(i,l) at l(l-1)/2 + i
+  double* col = sU + (size_t)k * (k - 1) / 2;        // T(0:k, j)
+  const int lane = threadIdx.x;
+  const int npair = j * (j + 1) / 2;  // entries with l <= j
+  for (int e = lane; e < npair; e += 32) sU[e] = vtv[e];
+  for (int i = lane; i < k; i += 32) col[i] = 0.0;
+  __syncwarp();
+  if (lane == 0) col[j] = tau[j];
+  __syncwarp();
+  for (int i = j - 1; i >= 0; --i) {
     const double ti = tau[i];
-    if (threadIdx.x < i) s_y[threadIdx.x] = -ti * vtv[i * (i - 1) / 2 + threadIdx.x];
-    __syncthreads();
     double acc = 0.0;
-    if (a < i && ti != 0.0)
-      for (int b = a + part; b < i; b += 4) acc = fma(sT[b * k + a], s_y[b], acc);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-    if (a < i && part == 0) sT[i * k + a] = acc;
-    if (threadIdx.x == 0) sT[i * k + i] = ti;
-    __syncthreads();
+    for (int l = i + 1 + lane; l <= j; l += 32) acc = fma(sU[l * (l - 1) / 2 + i], col[l], acc);
+    acc = warp_sum(acc);
+    if (lane == 0) col[i] = ti != 0.0 ? -ti * acc : 0.0;
+    __syncwarp();
   }
-  for (int e = threadIdx.x; e < k * k; e += blockDim.x) T[(size_t)(e / k) * ldt + (e % k)] = sT[e];
+  for (int i = lane; i < k; i += 32) T[(size_t)j * ldt + i] = col[i];
+}
+
+// Launch of k_larft for blocks of at most kmax reflectors.
+void launch_larft(const double* vtv, const double* tau, const BlockState* st, double* T, int kmax,
+                  cudaStream_t s) {
+  const size_t smem = sizeof(double) * ((size_t)kmax * (kmax - 1) / 2 + (size_t)kmax);
+  k_larft<<<kmax, 32, smem, s>>>(vtv, tau, st, T, kmax);
 }
 
 }  // namespace qrdm

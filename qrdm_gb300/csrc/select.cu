@@ -211,8 +211,18 @@ __global__ void k_gram_reduce(const double* __restrict__ part, int nchunk, int k
   if (nc <= 1) return;
   int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= km * km) return;
+  // fixed order; eight loads in flight ahead of the additions
+  const size_t stride = (size_t)km * km;
   double s = 0.0;
-  for (int c = 0; c < nchunk; ++c) s += part[(size_t)c * km * km + e];
+  int c = 0;
+  for (; c + 8 <= nchunk; c += 8) {
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) v[u] = __ldcg(part + (size_t)(c + u) * stride + e);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) s += v[u];
+  }
+  for (; c < nchunk; ++c) s += __ldcg(part + (size_t)c * stride + e);
   gram[e] = s;
 }
 
@@ -241,7 +251,19 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   double* s_g = reinterpret_cast<double*>(bits + ((nwords + 3) & ~3));  // [nc][nc] cosines
   const int nc = st->nc;
   for (int w = threadIdx.x; w < nwords; w += blockDim.x) bits[w] = 0u;
-  for (int e = threadIdx.x; e < nc * nc; e += blockDim.x) s_g[e] = gram[(size_t)(e / nc) * km + (e % nc)];
+  for (int base = 0; base < nc * nc; base += 8 * (int)blockDim.x) {  // 8 loads in flight per thread
+    double v[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * (int)blockDim.x + threadIdx.x;
+      v[u] = e < nc * nc ? __ldcg(gram + (size_t)(e / nc) * km + (e % nc)) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int e = base + u * (int)blockDim.x + threadIdx.x;
+      if (e < nc * nc) s_g[e] = v[u];
+    }
+  }
   __syncthreads();
   // greedy in norm order (warp 0): candidate i is taken iff every |cos| with
   // the columns taken so far is < delta; the max over taken columns is a
