@@ -37,6 +37,7 @@ struct BatchShared {
   double red[BT];
   double tw[KB];
   double sc[KB];
+  double sc_inv[KB];
   double jv_n[4 * KB + 8];
   int jv_j[4 * KB + 8];
   int2 perm[4 * KB + 8];
@@ -894,7 +895,10 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
     __syncthreads();
     BPH(1);
     // ---- panel (dgeqr2_mia) with early exit, columns scaled by 2^-e
-    for (int c = tid; c < fjb; c += blockDim.x) S.sc[c] = pow2_for(nrm[j + c]);
+    for (int c = tid; c < fjb; c += blockDim.x) {
+      S.sc[c] = pow2_for(nrm[j + c]);
+      S.sc_inv[c] = 1.0 / S.sc[c];
+    }
     if (tid == 0) {
       S.thres = 5e-14;
       S.exit_flag = 0;
@@ -923,14 +927,18 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
         S.scal = 0.0;
         S.beta = x[i];
         if (mloc - i > 1) {
+          // one thread: FP64 instructions are the latency, so the exact
+          // power-of-two scale is undone by multiplication and beta is
+          // formed directly from the scaled (overflow-safe) sum of squares
           const double xs = sqrt(S.red[0]);
-          if (i > 0 && xs / sci < S.thres) {
+          const double sinv = S.sc_inv[i];
+          if (i > 0 && xs * sinv < S.thres) {
             S.exit_flag = 1;
           } else if (xs != 0.0) {
-            const double bs = -sign_of(hypot_lapack(alpha, xs), alpha);
+            const double bs = -sign_of(sqrt(fma(alpha, alpha, S.red[0])), alpha);
             S.tau = (bs - alpha) / bs;
             S.scal = 1.0 / (alpha - bs);
-            S.beta = bs / sci;
+            S.beta = bs * sinv;
             S.tau_zero = 0;
           }
         }

@@ -32,6 +32,7 @@ namespace qrdm {
 
 struct PanelSmem {
   double sc[QRDM_NB_MAX];     // per-column scale 2^-e
+  double sc_inv[QRDM_NB_MAX]; // its exact inverse 2^e
   double tw[QRDM_NB_MAX];     // tau * w_c
   double red[QRDM_NB_MAX + 1];
   double tau, scal, beta, thres;
@@ -217,28 +218,37 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
   if (g == 0 && threadIdx.x == 0) p.st->fjb_cmp = kc;
 }
 
-// Partials for the clustered panel: one thread per slot, each summing its
-// dot product over this CTA's rows in two interleaved chains.  On GB300 an
-// FP64 warp instruction costs the SM's FP64 pipe the same whatever its
-// active lanes, so slots-across-lanes (no shuffle reductions) issues about a
-// fifth of the FP64 instructions of rows-across-lanes.  Columns are LS
-// (odd) doubles apart, so the 32 lanes' loads hit distinct banks.
+// Partials for the clustered panel: four threads per slot, each summing
+// every fourth row of this CTA's slab in two interleaved chains, combined
+// by a fixed shuffle tree.  Slots across threads (rather than rows across a
+// warp per slot) avoid a five-step FP64 shuffle reduction per slot, and four
+// threads per slot spread the FP64 instructions over all four SM
+// sub-partitions (one warp reaches a quarter of an SM's FP64 rate).
+// Columns are LS (odd) doubles apart, so the loads of different slots fall
+// in distinct banks.
 __device__ __forceinline__ void panel_partials_slots(const double* __restrict__ S, int LS, int nr, int grow0,
                                                     int i, int fjb, double* __restrict__ out) {
   const int nslot = fjb - i;
   int rr0 = i + 1 - grow0;  // first local row strictly below the diagonal
   if (rr0 < 0) rr0 = 0;
   const double* x = S + (size_t)i * LS;
-  for (int sl = threadIdx.x; sl < nslot; sl += blockDim.x) {
-    const double* y = S + (size_t)(i + sl) * LS;
+  const int part = threadIdx.x & 3;
+  for (int base = 0; base < nslot; base += (int)blockDim.x >> 2) {
+    const int sl = base + ((int)threadIdx.x >> 2);
     double a0 = 0.0, a1 = 0.0;
-    int rr = rr0;
-    for (; rr + 1 < nr; rr += 2) {
-      a0 = fma(x[rr], y[rr], a0);
-      a1 = fma(x[rr + 1], y[rr + 1], a1);
+    if (sl < nslot) {
+      const double* y = S + (size_t)(i + sl) * LS;
+      int rr = rr0 + part;
+      for (; rr + 4 < nr; rr += 8) {
+        a0 = fma(x[rr], y[rr], a0);
+        a1 = fma(x[rr + 4], y[rr + 4], a1);
+      }
+      if (rr < nr) a0 = fma(x[rr], y[rr], a0);
     }
-    if (rr < nr) a0 = fma(x[rr], y[rr], a0);
-    out[sl] = a0 + a1;
+    double acc = a0 + a1;
+    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
+    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
+    if (sl < nslot && part == 0) out[sl] = acc;
   }
 }
 
@@ -274,7 +284,10 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
   const int stride = QRDM_NB_MAX + 1;
   const int tid = threadIdx.x;
 
-  for (int c = tid; c < fjb; c += blockDim.x) sm.sc[c] = pow2_scale_for(p.nrm[c]);
+  for (int c = tid; c < fjb; c += blockDim.x) {
+    sm.sc[c] = pow2_scale_for(p.nrm[c]);
+    sm.sc_inv[c] = 1.0 / sm.sc[c];
+  }
   if (tid == 0) {
     sm.exit_flag = 0;
     sm.thres = 5e-14;
@@ -388,7 +401,6 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     PPH(3);
     // 4. dlarfg scalars (thread 0), then w_c in parallel
     if (tid == 0) {
-      const double sci = sm.sc[i];
       const double alpha = s_row[i];
       const int order = p.mloc - i;
       sm.tau_zero = 1;
@@ -396,12 +408,17 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
       sm.scal = 0.0;
       sm.beta = alpha;
       if (order > 1) {
-        double xs = sqrt(sm.red[0]);
-        double xnorm = xs / sci;
+        // one thread on one SM sub-partition: FP64 instructions are the
+        // latency here, so the power-of-two scale is undone by multiplying
+        // with its exact inverse and beta = -sign(alpha) sqrt(alpha^2 + xs^2)
+        // is formed directly (the scaled column keeps both terms far from
+        // overflow and underflow)
+        const double xs = sqrt(sm.red[0]);
+        const double xnorm = xs * sm.sc_inv[i];
         if (i > 0 && p.allow_exit && xnorm < sm.thres) {
           sm.exit_flag = 1;
         } else if (xs != 0.0) {
-          double beta = -sign_of(hypot_lapack(alpha, xs), alpha);
+          const double beta = -sign_of(sqrt(fma(alpha, alpha, sm.red[0])), alpha);
           sm.tau = (beta - alpha) / beta;
           sm.scal = 1.0 / (alpha - beta);
           sm.beta = beta;
@@ -409,7 +426,7 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
         }
       }
       if (!sm.exit_flag) {
-        if (i == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(sm.beta / sci);
+        if (i == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(sm.beta) * sm.sc_inv[0];
         if (g == 0) p.tau[i] = sm.tau;
       }
     }
