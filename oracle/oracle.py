@@ -61,12 +61,21 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
+# where build_ref.sh finds the reference sources (present only in the
+# container that holds them; never on the GPU machine)
+REFERENCE_ROOT = os.environ.get("QRDM_REFERENCE_ROOT", "/root/reference")
+
+
+def reference_sources_present() -> bool:
+    return os.path.isdir(os.path.join(REFERENCE_ROOT, "src"))
+
+
 def build_reference() -> str | None:
     """Compile the unmodified reference sources (only where they exist)."""
     script = os.path.join(HERE, "build_ref.sh")
-    if not os.path.isdir("/root/reference/src"):
+    if not reference_sources_present():
         return None
-    subprocess.check_call(["bash", script])
+    subprocess.check_call(["bash", script, REFERENCE_ROOT])
     return REF_SO if os.path.exists(REF_SO) else None
 
 

@@ -51,7 +51,8 @@ def test_qp3_oracle_matches_fixture(oracle, qp3_golden):
         assert np.linalg.norm(A - c["A_out"]) <= 1e-12 * np.linalg.norm(c["A_in"]), name
 
 
-@pytest.mark.skipif(not os.path.isdir("/root/reference/src"), reason="reference sources absent")
+@pytest.mark.skipif(not __import__("oracle.oracle", fromlist=["x"]).reference_sources_present(),
+                    reason="reference sources absent")
 @pytest.mark.parametrize("shape,seed,nb", [((300, 200), 3, 64), ((200, 300), 4, 32),
                                            ((1000, 1000), 0, 64), ((257, 129), 5, 17)])
 def test_oracle_bit_exact_vs_compiled_reference(oracle, shape, seed, nb):
