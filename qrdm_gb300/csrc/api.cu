@@ -360,7 +360,10 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     CK(cudaMemsetAsync(d_st, 0, sizeof(BlockState), s));
     PH(0);
     // ---- DM candidates (DM_perm :345-351)
-    if (nloc <= kTopkFinal) {
+    if (nloc <= kTopkRadixMax) {
+      launch_topk_radix(nloc, s, nrm + j, kmax, P.tau_rel, c.cand.as<Cand>(), d_st);
+      RET(check_launch());
+    } else if (nloc <= kTopkFinal) {
       launch_topk_final(nloc, s, nullptr, nrm + j, kmax, P.tau_rel, c.cand.as<Cand>(), d_st);
       RET(check_launch());
     } else {

@@ -794,11 +794,15 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
         S.pos[0] = 0;
       }
       __syncwarp();
+      const unsigned long long delta_bits = abs_bits(a.delta);
       for (int i = 1; i < nc; ++i) {
-        double worst = 0.0;
-        for (int q = lane; q < nsel; q += 32) worst = fmax(worst, fabs(S.g[S.pos[q] * GS + i]));
-        worst = warp_max(worst);
-        if (worst < a.delta && nsel < kmax) {
+        unsigned long long worst = 0ull;  // max |cos| as bits (integer pipes)
+        for (int q = lane; q < nsel; q += 32) {
+          const unsigned long long b = abs_bits(S.g[S.pos[q] * GS + i]);
+          worst = b > worst ? b : worst;
+        }
+        worst = warp_max_u64(worst);
+        if (worst < delta_bits && nsel < kmax) {
           if (lane == 0) {
             S.pos[nsel] = i;
             S.sel[nsel] = S.cand[i].idx;

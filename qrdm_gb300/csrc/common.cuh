@@ -40,6 +40,22 @@ __device__ __forceinline__ double warp_max(double v) {
   return v;
 }
 
+// |x| of a double as its bit pattern: for non-negative doubles the unsigned
+// order of the bits is the numeric order, so maxima and threshold tests on
+// |cos| run on the integer pipes (an FP64 warp instruction costs one SM
+// sub-partition 16x the cycles of an integer one on GB300).
+__device__ __forceinline__ unsigned long long abs_bits(double x) {
+  return (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+}
+__device__ __forceinline__ unsigned long long warp_max_u64(unsigned long long v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w > v ? w : v;
+  }
+  return v;
+}
+
 // Non-contracted multiply-add (keeps the rounding of a separate mul + add,
 // the way the reference's C loops round on x86-64).
 __device__ __forceinline__ double mul_add_rn(double a, double b, double c) {

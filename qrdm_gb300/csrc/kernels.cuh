@@ -61,6 +61,9 @@ __global__ void k_norm_recompute(const double* A, long long lda, int j, int m, c
 // select.cu
 __global__ void k_topk_tile(const double* nrm, const Cand* in_cand, int count, int kmax,
                             Cand* out);
+constexpr int kTopkRadixMax = 65536;  // largest count the radix top-k takes
+void launch_topk_radix(int count, cudaStream_t s, const double* nrm, int kmax, double tau_rel, Cand* cand,
+                       BlockState* st);
 void launch_topk_final(int count, cudaStream_t st_, const Cand* in_cand, const double* nrm, int kmax,
                        double tau_rel, Cand* cand, BlockState* st);
 void launch_gram_partial(int km, int nchunk, cudaStream_t s, const double* A, long long lda, int j,

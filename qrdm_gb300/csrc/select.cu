@@ -50,6 +50,177 @@ __device__ void bitonic_sort(Cand* s) {
   }
 }
 
+// Bitonic sort of s[0..n) for a power of two n <= 1024 chosen at run time.
+__device__ void bitonic_sort_n(Cand* s, int n) {
+  for (int k = 2; k <= n; k <<= 1) {
+    for (int jj = k >> 1; jj > 0; jj >>= 1) {
+      for (int t = threadIdx.x; t < n / 2; t += blockDim.x) {
+        int lo = 2 * jj * (t / jj) + (t % jj);
+        int hi = lo + jj;
+        bool up = ((lo & k) == 0);
+        Cand a = s[lo], b = s[hi];
+        bool swap = up ? cand_before(b, a) : cand_before(a, b);
+        if (swap) {
+          s[lo] = b;
+          s[hi] = a;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// K-topk by radix selection (one CTA, count <= kTopkRadixMax): partial norms
+// are non-negative doubles, so their bit patterns order like their values.
+// Histogram passes over 8-bit digits (most significant first) narrow the
+// key range holding the kmax-th largest value until the entries at or above
+// it fit the 512-entry list; those are sorted by (value desc, index asc),
+// the reference's order.  When equal values straddle the cut even after the
+// last digit (e.g. many zero norms), the ties are taken in index order by a
+// block-wide prefix count.  Writes cand[0..kmax) and nc, like k_topk_final.
+constexpr int kTopkList = 512;
+
+__global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ nrm, int count, int kmax,
+                                                     double tau_rel, Cand* __restrict__ cand,
+                                                     BlockState* __restrict__ st) {
+  __shared__ unsigned hist[256];
+  __shared__ Cand list[kTopkList];
+  __shared__ int s_nlist, s_above, s_d;
+  __shared__ int s_scan[32];
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int want = min(kmax, count);
+  unsigned long long prefix = 0ull, mask = 0ull;
+  int need = want;  // entries still to take from the current bucket
+  int above = 0;    // entries strictly above the current bucket
+  bool small = count <= kTopkList;
+  for (int shift = 56; shift >= 0 && !small; shift -= 8) {
+    for (int b = tid; b < 256; b += blockDim.x) hist[b] = 0u;
+    __syncthreads();
+    for (int i = tid; i < count; i += blockDim.x) {
+      const unsigned long long key = (unsigned long long)__double_as_longlong(nrm[i]);
+      if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
+    }
+    __syncthreads();
+    if (w == 0) {
+      // lane l holds bins 255-8l .. 248-8l (descending); find the digit d
+      // whose bucket contains the need-th entry from the top
+      unsigned c[8];
+      unsigned sum = 0;
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        c[q] = hist[255 - 8 * lane - q];
+        sum += c[q];
+      }
+      unsigned incl = sum;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const unsigned v = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += v;
+      }
+      const unsigned excl = incl - sum;
+      const bool here = excl < (unsigned)need && incl >= (unsigned)need;
+      if (here) {
+        unsigned run = excl;
+        for (int q = 0; q < 8; ++q) {
+          if (run + c[q] >= (unsigned)need) {
+            s_d = 255 - 8 * lane - q;
+            s_above = (int)run;
+            break;
+          }
+          run += c[q];
+        }
+      }
+    }
+    __syncthreads();
+    const int d = s_d;
+    above += s_above;
+    need -= s_above;
+    prefix |= (unsigned long long)d << shift;
+    mask |= 0xFFull << shift;
+    if (above + (int)hist[d] <= kTopkList) small = true;
+    __syncthreads();
+  }
+  if (tid == 0) s_nlist = 0;
+  __syncthreads();
+  if (small) {
+    // every entry at or above the bucket fits the list
+    for (int i = tid; i < count; i += blockDim.x) {
+      const double v = nrm[i];
+      const unsigned long long key = (unsigned long long)__double_as_longlong(v);
+      if ((key & mask) >= prefix) {
+        const int slot = atomicAdd(&s_nlist, 1);
+        if (slot < kTopkList) list[slot] = Cand{v, i, 0};
+      }
+    }
+  } else {
+    // exact cut value with too many equal entries: all above it, then the
+    // `need` equal ones of smallest index (contiguous index ranges per
+    // thread, block-wide exclusive prefix count of the ties)
+    const int chunk = ceil_div(count, (int)blockDim.x);
+    const int i0 = tid * chunk, i1 = min(count, i0 + chunk);
+    int ties = 0;
+    for (int i = i0; i < i1; ++i) {
+      const double v = nrm[i];
+      const unsigned long long key = (unsigned long long)__double_as_longlong(v);
+      if (key > prefix) {
+        const int slot = atomicAdd(&s_nlist, 1);
+        if (slot < kTopkList) list[slot] = Cand{v, i, 0};
+      } else if (key == prefix) {
+        ++ties;
+      }
+    }
+    int incl = ties;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) s_scan[w] = incl;
+    __syncthreads();
+    if (w == 0) {
+      const int nwarp = (int)blockDim.x >> 5;
+      int v = lane < nwarp ? s_scan[lane] : 0;
+      int x = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      if (lane < nwarp) s_scan[lane] = x - v;  // exclusive over warps
+    }
+    __syncthreads();
+    int rank = s_scan[w] + incl - ties;
+    for (int i = i0; i < i1 && rank < need; ++i) {
+      const double v = nrm[i];
+      const unsigned long long key = (unsigned long long)__double_as_longlong(v);
+      if (key == prefix) {
+        const int slot = atomicAdd(&s_nlist, 1);
+        if (slot < kTopkList) list[slot] = Cand{v, i, 0};
+        ++rank;
+      }
+    }
+  }
+  __syncthreads();
+  const int nlist = min(s_nlist, kTopkList);
+  int n2 = 64;
+  while (n2 < nlist) n2 <<= 1;
+  for (int t = nlist + tid; t < n2; t += blockDim.x) list[t] = Cand{-1.0, 0x7fffffff, 0};
+  __syncthreads();
+  bitonic_sort_n(list, n2);
+  for (int t = tid; t < kmax; t += blockDim.x) cand[t] = t < want ? list[t] : Cand{-1.0, 0x7fffffff, 0};
+  if (tid == 0) {
+    const double cut = tau_rel * list[0].val;
+    int nc = 0;
+    while (nc < want && list[nc].val > cut) ++nc;
+    st->nc = nc;
+  }
+}
+
+void launch_topk_radix(int count, cudaStream_t s, const double* nrm, int kmax, double tau_rel, Cand* cand,
+                       BlockState* st) {
+  k_topk_radix<<<1, 1024, 0, s>>>(nrm, count, kmax, tau_rel, cand, st);
+}
+
 constexpr int TOPK_TILE = kTopkTile;
 
 // Each CTA sorts TOPK_TILE entries and keeps its first kmax.
@@ -276,11 +447,15 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
       s_pos[0] = 0;
     }
     __syncwarp();
+    const unsigned long long delta_bits = abs_bits(delta);
     for (int i = 1; i < nc; ++i) {
-      double worst = 0.0;
-      for (int q = lane; q < nsel; q += 32) worst = fmax(worst, fabs(s_g[s_pos[q] * nc + i]));
-      worst = warp_max(worst);
-      if (worst < delta && nsel < kmax) {
+      unsigned long long worst = 0ull;  // max |cos| as bits (integer pipes)
+      for (int q = lane; q < nsel; q += 32) {
+        const unsigned long long b = abs_bits(s_g[s_pos[q] * nc + i]);
+        worst = b > worst ? b : worst;
+      }
+      worst = warp_max_u64(worst);
+      if (worst < delta_bits && nsel < kmax) {
         if (lane == 0) {
           s_pos[nsel] = i;
           s_sel[nsel] = cand[i].idx;

@@ -151,3 +151,22 @@ def test_repeatable_bits(gpu_lib):
     b = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
     assert np.array_equal(a["A"], b["A"]) and np.array_equal(a["tau"], b["tau"])
     assert np.array_equal(a["jpvt"], b["jpvt"])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_many_equal_norms(gpu_lib, oracle, precision):
+    """Candidate selection when more than 512 columns share the cut value
+    (1340 exactly zero columns next to 60 live ones): the ties are taken in
+    index order, as the reference's stable sort does."""
+    import qrdm_gb300
+
+    rng = np.random.default_rng(17)
+    m, n = 96, 1400
+    A0 = np.zeros((m, n), order="F")
+    live = rng.choice(n, size=60, replace=False)
+    A0[:, live] = rng.standard_normal((m, 60)) * np.exp(rng.uniform(0, 3, 60))
+    prefix, ref = separated(oracle, A0, (0.9, 0.15, 32, 0, 0.0))
+    assert prefix[1] >= 96, prefix  # zero columns decide nothing: the whole run is separated
+    gpu = run_gpu(A0, (0.9, 0.15, 32, 0, 0.0), precision=precision)
+    check_against(A0, gpu, ref, prefix, label=f"ties-{precision}")
