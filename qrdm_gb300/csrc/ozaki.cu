@@ -467,12 +467,12 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
 // ------------------------------------------------------------- GEMM 2
 // C(r, c) -= V(r, :) W2(:, c), persistent and pipelined.  Work items are
 // 128-row x 32-column tiles of C in band-major order; each CTA takes a
-// contiguous range.  Warp 8 (one lane) is the producer and MMA issuer: it
-// keeps the V digits of the current 128-row band resident (one bulk copy per
-// band), streams the W2 digits of each 32-column tile through a ring of
-// NST2 stages (bulk copies), and accumulates each tile's S levels into one
-// of two TMEM buffers.  Warps 0..7 are the epilogue: each owns 32 rows
-// (its TMEM lane quadrant) x 16 columns of a tile, loads its C entries
+// contiguous range.  The last warp (one lane) is the producer and MMA
+// issuer: it keeps the V digits of the current 128-row band resident (one
+// bulk copy per band), streams the W2 digits of each 32-column tile through
+// a ring of NST2 stages (bulk copies), and accumulates each tile's S levels
+// into one of two TMEM buffers.  The other sixteen warps are the epilogue:
+// each owns 32 rows (its TMEM lane quadrant) x 8 columns of a tile, loads its C entries
 // before the tile's MMAs finish, recombines the levels and writes C back,
 // then frees the TMEM buffer, so the next tile's MMAs overlap this tile's
 // epilogue.
@@ -486,7 +486,9 @@ struct OzG2Args {
   BlockState* st;
 };
 
-constexpr int OZ_G2_THREADS = 288;  // 8 epilogue warps + 1 producer warp
+constexpr int OZ_G2_EPI = 16;                          // epilogue warps
+constexpr int OZ_G2_THREADS = 32 * (OZ_G2_EPI + 1);   // + 1 producer warp
+constexpr int OZ_G2_CPW = 32 / (OZ_G2_EPI / 4);        // tile columns per epilogue warp
 constexpr int NST2 = 3;              // W2 digit stages
 
 template <int S>
@@ -517,7 +519,7 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
     }
     for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&tfull[i], 1);
-      tc::mbar_init(&tempty[i], 8);
+      tc::mbar_init(&tempty[i], OZ_G2_EPI);
     }
     tc::fence_mbar_init();
   }
@@ -527,7 +529,7 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
   bool fail = false;
-  if (w == 8) {
+  if (w == OZ_G2_EPI) {
     if (lane == 0) {
       auto produce = [&](int kk) {
         const int it = first + kk, t = it % ntile, stg = kk % NST2;
@@ -578,27 +580,28 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
         tc::mbar_wait(&empty[kk % NST2], (uint32_t)((kk / NST2) & 1));
     }
   } else {
-    // epilogue: rows 32 (w & 3) + lane of the band, columns 16 (w >> 2) + j,
-    // in two groups of 8 columns
+    // epilogue: rows 32 (w & 3) + lane of the band, CPW columns from
+    // CPW (w >> 2): four warps per TMEM lane quadrant keep every SM
+    // sub-partition's FP64 pipe fed with the final conversions and FMAs
     const int quad = w & 3, ch = w >> 2;
     const uint32_t tl = tmem + ((uint32_t)(32 * quad) << 16);
     for (int kk = 0; kk < nmine; ++kk) {
       const int it = first + kk, band = it / ntile, t = it % ntile, b = kk & 1;
       const int r = band * 128 + 32 * quad + lane;
-      const int cw0 = t * 32 + 16 * ch;  // C column relative to fjb
-      double cv[16];
+      const int cw0 = t * 32 + OZ_G2_CPW * ch;  // C column relative to fjb
+      double cv[OZ_G2_CPW];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
+      for (int j = 0; j < OZ_G2_CPW; ++j) {
         const int c = fjb + cw0 + j;
         cv[j] = (r < g.mloc && c < g.ncols) ? g.W0[(size_t)c * g.lda + r] : 0.0;
       }
       if (!tc::mbar_wait(&tfull[b], (uint32_t)((kk >> 1) & 1))) fail = true;
       tc::fence_after_sync();
 #pragma unroll
-      for (int jb = 0; jb < 16; jb += 8) {
+      for (int jb = 0; jb < OZ_G2_CPW; jb += 8) {
         long long hi[8], mid[8];
-        oz_levels8<S>(tl + (uint32_t)(b * 256), 0, hi, mid, (uint32_t)(16 * ch + jb));
-        if (jb == 8) {
+        oz_levels8<S>(tl + (uint32_t)(b * 256), 0, hi, mid, (uint32_t)(OZ_G2_CPW * ch + jb));
+        if (jb + 8 >= OZ_G2_CPW) {
           tc::fence_before_sync();
           __syncwarp();
           if (lane == 0) tc::mbar_arrive(&tempty[b]);

@@ -451,12 +451,23 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
       double* x = S + (size_t)i * LS;
       for (int rr = rr0 + tid; rr < nr; rr += blockDim.x) x[rr] *= scal;
       __syncthreads();
-      for (int e = tid; e < ncol_r * nr; e += blockDim.x) {
-        int cc = e / nr, rr = e % nr;
-        int c = i + 1 + cc;
-        int grow = grow0 + rr;
-        if (grow > i) S[(size_t)c * LS + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * LS + rr]);
-        else if (grow == i) S[(size_t)c * LS + rr] -= sm.tw[c];
+      // flattened (column, row) index over all threads, advanced by a
+      // precomputed step instead of a division per entry
+      if (nr > 0) {
+        int cc = tid / nr, rr = tid % nr;
+        const int dc = (int)blockDim.x / nr, dr = (int)blockDim.x % nr;
+        for (; cc < ncol_r; ) {
+          const int c = i + 1 + cc;
+          const int grow = grow0 + rr;
+          if (grow > i) S[(size_t)c * LS + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * LS + rr]);
+          else if (grow == i) S[(size_t)c * LS + rr] -= sm.tw[c];
+          rr += dr;
+          cc += dc;
+          if (rr >= nr) {
+            rr -= nr;
+            ++cc;
+          }
+        }
       }
       if (grow0 <= i && i < grow0 + nr && tid == 0) x[i - grow0] = sm.beta;
     }
