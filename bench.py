@@ -285,7 +285,7 @@ def run_ours(args):
         work.copy_(pristine)
         jp.zero_()
         nc = np.zeros(n, np.int32)
-        opt = default_options(precision=precision, kstop=KSTOP.get(args.workload, 0))
+        opt = default_options(precision=precision, kstop=KSTOP.get(args.workload, 0), slices=args.slices)
         st = stats if stats is not None else Stats()
         info = L.dgeqrdm_dev(102, m, n, C.c_void_p(work.data_ptr()), m, C.c_void_p(jp.data_ptr()),
                              C.c_void_p(tau.data_ptr()), nc.ctypes.data_as(C.POINTER(C.c_int)),
@@ -328,7 +328,7 @@ def run_ours(args):
         # launching stream) for the roofline of the dominant phase
         sti = Stats()
         sti.timing = 1
-        step(sti)
+        _, nc_i = step(sti)
         peaks, peak_kind = load_peaks()
         phase = {"select": sti.ms_select, "panel": sti.ms_panel, "tfactor": sti.ms_tfactor,
                  "trail": sti.ms_trail, "norm": sti.ms_norm}
@@ -352,7 +352,7 @@ def run_ours(args):
         else:
             # Ozaki split: s digits per operand, the s (s + 1) / 2 digit
             # products of level <= s + 1 are BF16 GEMMs of the FP64 shape
-            s_dig = int(default_options().slices) or 7
+            s_dig = int(args.slices or default_options().slices) or 7
             prods = s_dig * (s_dig + 1) // 2
             tflop = sti.trail_flops * prods
             achieved = tflop / (sti.ms_trail / 1e3) / 1e12 if sti.ms_trail > 0 else 0.0
@@ -371,6 +371,33 @@ def run_ours(args):
                                         f"block, {nblk} blocks",
                     "fp64_equivalent_tflops": (sti.trail_flops / (sti.ms_trail / 1e3) / 1e12
                                                if sti.ms_trail > 0 else 0.0)}
+        # accuracy of the instrumented factorisation, on the device:
+        # ||A P - Q R||_F / ||A||_F with Q R formed by the library's DORMQR,
+        # and the |R_kk| profile
+        accuracy = None
+        try:
+            k = int(np.sum(nc_i[:int(np.count_nonzero(nc_i))])) if KSTOP.get(args.workload) else min(m, n)
+            k = min(k, m, n)
+            Af = work.T  # m x n view of the column-major factor
+            R = torch.zeros_like(Af)
+            R[:k, :] = torch.triu(Af[:k, :])
+            if k < min(m, n):
+                R[k:, k:] = Af[k:, k:]
+            QR = R.T.contiguous()  # column-major m x n
+            rq = L.qrdm_dormqr_dev(102, m, n, k, C.c_void_p(work.data_ptr()), m, C.c_void_p(tau.data_ptr()),
+                                   C.c_void_p(QR.data_ptr()), m)
+            if rq == 0:
+                p = (jp.long() - 1)
+                be = float(torch.linalg.norm(QR - pristine[p]) / torch.linalg.norm(pristine))
+                rd = torch.abs(torch.diagonal(Af)[:k]).cpu().numpy()
+                r0 = float(rd[0]) if rd.size else 0.0
+                accuracy = {"backward": be, "backward_bound_10_n_eps": 10 * max(m, n) * 2.0 ** -53,
+                            "rkk_first": r0, "rkk_at": {str(i): float(rd[i]) for i in
+                                                        (min(k - 1, 2047), min(k - 1, 2048), k - 1)},
+                            "numerical_rank_1e-8": int(np.count_nonzero(rd > 1e-8 * r0))}
+            del R, QR
+        except Exception as exc:  # accuracy is reported, never fatal for the timing
+            accuracy = {"error": str(exc)[:200]}
         # e2e through the host C ABI with pinned host buffers
         a_host = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
         a_host.copy_(pristine)
@@ -383,7 +410,7 @@ def run_ours(args):
             a_np[...] = src
             jp_h[:] = 0
             nc = np.zeros(n, np.int32)
-            opt = default_options(precision=prec, kstop=KSTOP.get(args.workload, 0))
+            opt = default_options(precision=prec, kstop=KSTOP.get(args.workload, 0), slices=args.slices)
             st = Stats()
             t0 = time.perf_counter()
             info = L.dgeqrdm_ex(102, m, n, a_np.ctypes.data_as(pd), m,
@@ -446,11 +473,11 @@ def run_ours(args):
                "data": "synthetic",
                "config": {"workload": args.workload, "m": m, "n": n, "nb": NB, "delta": DELTA,
                           "tau_": TAU_, "precision": args.precision, "matrix": desc,
-                          "kstop": KSTOP.get(args.workload, 0),
+                          "kstop": KSTOP.get(args.workload, 0), "slices": args.slices or None,
                           "parallelism": f"replicas{world}",
                           "l2": "inputs (8 m n bytes) larger than L2; no flush needed"},
                "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": launches, "clocks": clocks, "variants": variants}
+               "gpu_launches": launches, "clocks": clocks, "accuracy": accuracy, "variants": variants}
         print(json.dumps(out), flush=True)
     barrier(world)
     if world > 1:
@@ -729,6 +756,8 @@ def main():
     ap.add_argument("--no-variants", dest="variants", action="store_false")
     ap.add_argument("--count", type=int, default=None,
                     help="batched2000: number of problems (default 2000)")
+    ap.add_argument("--slices", type=int, default=0,
+                    help="mixed precision: digits per operand of the Ozaki split (0: library default)")
     ap.add_argument("--batch-nb", type=int, default=0,
                     help="batched2000: DM block size (0: autotuner picks nb and precision)")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
