@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -239,33 +240,65 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
 static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
                          int* hj, int* err);
 
+// Shapes of the clustered panel on this device.  The dynamic shared memory
+// is raised past half of an SM's, so no SM ever holds two panel CTAs (with
+// smaller requests the scheduler packs clusters two CTAs to an SM inside a
+// GPC, doubling the FP64 work on those SMs); then the co-resident cluster
+// count is recorded for clusters of 1, 2, 4 and 8 CTAs.  QRDM_PANEL_CLUSTER
+// = 1, 2, 4 or 8 pins the cluster size (tuning).
+static void choose_panel_clusters(Ctx& c) {
+  int per_sm = 0;
+  if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.dev) != cudaSuccess)
+    per_sm = 0;
+  size_t floor_b = (size_t)per_sm / 2 + 1024;
+  if (floor_b + 8192 > c.smem_optin) floor_b = 0;
+  c.pan_smem_floor = std::max<size_t>(floor_b, 1);
+  for (int ci = 0; ci < 4; ++ci) c.pan_cap[ci] = panel_cluster_capacity(c.pan_smem_floor, 1 << ci);
+  const char* f = getenv("QRDM_PANEL_CLUSTER");
+  const int v = f ? atoi(f) : 0;
+  c.pan_cs_force = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
+}
+
 // Launch the Householder panel on the window of pa: the clustered kernel
 // when the device can co-schedule enough 8-CTA clusters, else the plain
 // cooperative kernel.  *G_used receives the number of CTAs (the count of
 // V^T V partials).
 static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t s, int* G_used) {
+  if (c.pan_smem_floor == 0) choose_panel_clusters(c);
   const int g0 = panel_ctas(mloc, c.nsm);
-  int ncl = ceil_div(g0, kPanelClusterSize);
-  for (int attempt = 0; attempt < 3 && ncl > 0; ++attempt) {
-    const int G = ncl * kPanelClusterSize;
-    const int R = ceil_div(mloc, G);
-    const size_t smem = (size_t)(R | 1) * kmax * sizeof(double);  // odd slab stride
-    if (smem + 8192 > c.smem_optin) break;
-    const int cap = panel_cluster_capacity(smem);
-    if (cap <= 0) break;
-    if (ncl > cap) {
-      ncl = cap;
-      continue;
+  // The panel's critical path is the FP64 work of one CTA per column: its
+  // rows' update and partial dot products (2 R per slot) plus the
+  // fixed-order sum of the ncl cluster totals (ncl per slot) that every CTA
+  // repeats.  Take the cluster size with the least of it among the shapes
+  // that fit one CTA per SM.
+  int best_cs = 0, best_G = 0;
+  long long best_cost = 0;
+  for (int ci = 0; ci < 4; ++ci) {
+    const int cs = 1 << ci;
+    if (c.pan_cs_force && cs != c.pan_cs_force) continue;
+    const int ncl = std::min(ceil_div(g0, cs), c.pan_cap[ci]);
+    if (ncl <= 0) continue;
+    const int G = ncl * cs, R = ceil_div(mloc, G);
+    const size_t need = (size_t)(R | 1) * kmax * sizeof(double);  // odd slab stride
+    if (need + 8192 > c.smem_optin) continue;
+    const long long cost = 2ll * R + ncl;
+    if (best_cs == 0 || cost < best_cost || (cost == best_cost && cs > best_cs)) {
+      best_cs = cs;
+      best_G = G;
+      best_cost = cost;
     }
+  }
+  if (best_cs > 0) {
+    const int G = best_G, R = ceil_div(mloc, G);
+    const size_t smem = std::max((size_t)(R | 1) * kmax * sizeof(double), c.pan_smem_floor);
     pa.rows_per_cta = R;
     CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
-    if (launch_panel_cluster(pa, G, smem, s) == cudaSuccess) {
+    if (launch_panel_cluster(pa, G, best_cs, smem, s) == cudaSuccess) {
       ++g_launches;
       *G_used = G;
       return 0;
     }
     cudaGetLastError();  // clear, fall back below
-    break;
   }
   int G = 1, R = 1;
   size_t psmem = 0;

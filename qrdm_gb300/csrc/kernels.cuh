@@ -86,9 +86,9 @@ __global__ void k_vtv_stored(const double* V, long long ldv, int mloc, int rows_
                              const BlockState* st, double* vtv_part);
 __global__ void k_panel(PanelArgs p);
 __global__ void k_panel_cluster(PanelArgs p);
-cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, size_t smem, cudaStream_t s);
-int panel_cluster_capacity(size_t smem);
-constexpr int kPanelClusterSize = 8;
+cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, int cs, size_t smem, cudaStream_t s);
+int panel_cluster_capacity(size_t smem, int cs);
+constexpr int kPanelClusterSize = 8;  // largest panel cluster (1, 2, 4 or 8 CTAs)
 __global__ void k_vtv_reduce(const double* vtv_part, int G, const BlockState* st, double* vtv);
 __global__ void k_larft(const double* vtv, const double* tau, const BlockState* st, double* T,
                         int ldt);

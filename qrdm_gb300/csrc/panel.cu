@@ -35,7 +35,7 @@ struct PanelSmem {
   double sc_inv[QRDM_NB_MAX]; // its exact inverse 2^e
   double tw[QRDM_NB_MAX];     // tau * w_c
   double red[QRDM_NB_MAX + 1];
-  double tau, scal, beta, thres;
+  double tau, scal, beta, thres, rbeta;
   int exit_flag, tau_zero;
 };
 
@@ -253,14 +253,15 @@ __device__ __forceinline__ void panel_partials_slots(const double* __restrict__ 
 }
 
 // ------------------------------------------------ clustered panel (K-panel)
-// Same arithmetic as k_panel, launched as clusters of kPanelCluster CTAs:
+// Same arithmetic as k_panel, launched as clusters of 1, 2, 4 or 8 CTAs:
 // per column, each CTA's partial slots are summed by its cluster leader
 // through distributed shared memory (fixed order), the leaders publish
 // cluster totals and advance a global counter, every CTA spins (bounded) on
 // that counter and then sums the nclusters totals in a fixed order, so all
 // CTAs hold bit-identical scalars.  The w_c of the reflector application are
 // formed by one thread per column.
-constexpr int kPanelCluster = 8;
+constexpr int kPanelCluster = kPanelClusterSize;
+constexpr int kCrossLoads = 10;  // cluster totals in flight per thread (4 threads per slot)
 
 __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -381,15 +382,15 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
       const int sl = base + (tid >> 2), q0 = tid & 3;
       double acc = 0.0;
       if (sl < nslot) {
-        for (int qb = q0; qb < ncl; qb += 32) {
-          double v[8];
+        for (int qb = q0; qb < ncl; qb += 4 * kCrossLoads) {
+          double v[kCrossLoads];
 #pragma unroll
-          for (int u = 0; u < 8; ++u) {
+          for (int u = 0; u < kCrossLoads; ++u) {
             const int q = qb + 4 * u;
             v[u] = q < ncl ? __ldcg(part + (size_t)q * stride + sl) : 0.0;
           }
 #pragma unroll
-          for (int u = 0; u < 8; ++u)
+          for (int u = 0; u < kCrossLoads; ++u)
             if (qb + 4 * u < ncl) acc += v[u];
         }
       }
@@ -399,36 +400,28 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     }
     __syncthreads();
     PPH(3);
-    // 4. dlarfg scalars (thread 0), then w_c in parallel
+    // 4. dlarfg scalars.  FP64 instructions with one active lane still take
+    //    the SM sub-partition's FP64 pipe for a whole warp's time, so the
+    //    chain is kept short and split across warps on different
+    //    sub-partitions: beta first (thread 0; the exit test compares
+    //    squares, no square root), then 1/beta and tau (warp 0) beside
+    //    1/(alpha - beta) (warp 1), then tau w_c = tau C(i,c) - (x.C_c)/beta
+    //    (tau / (alpha - beta) = -1/beta) beside the scaling of x.
     if (tid == 0) {
-      const double alpha = s_row[i];
-      const int order = p.mloc - i;
+      const double alpha = s_row[i], red0 = sm.red[0];
       sm.tau_zero = 1;
-      sm.tau = 0.0;
-      sm.scal = 0.0;
       sm.beta = alpha;
-      if (order > 1) {
-        // one thread on one SM sub-partition: FP64 instructions are the
-        // latency here, so the power-of-two scale is undone by multiplying
-        // with its exact inverse and beta = -sign(alpha) sqrt(alpha^2 + xs^2)
-        // is formed directly (the scaled column keeps both terms far from
-        // overflow and underflow)
-        const double xs = sqrt(sm.red[0]);
-        const double xnorm = xs * sm.sc_inv[i];
-        if (i > 0 && p.allow_exit && xnorm < sm.thres) {
+      if (p.mloc - i > 1) {
+        const double t = sm.thres * sm.sc[i];  // thres in this column's scaled units
+        if (i > 0 && p.allow_exit && red0 < t * t) {
           sm.exit_flag = 1;
-        } else if (xs != 0.0) {
-          const double beta = -sign_of(sqrt(fma(alpha, alpha, sm.red[0])), alpha);
-          sm.tau = (beta - alpha) / beta;
-          sm.scal = 1.0 / (alpha - beta);
-          sm.beta = beta;
+        } else if (red0 != 0.0) {
+          sm.beta = -sign_of(sqrt(fma(alpha, alpha, red0)), alpha);
           sm.tau_zero = 0;
         }
       }
-      if (!sm.exit_flag) {
-        if (i == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(sm.beta) * sm.sc_inv[0];
-        if (g == 0) p.tau[i] = sm.tau;
-      }
+      if (!sm.exit_flag && i == 0 && fjb > 1 && p.tau_rel > 0.0)
+        sm.thres = p.tau_rel * fabs(sm.beta) * sm.sc_inv[0];
     }
     __syncthreads();
     if (sm.exit_flag == 1) {
@@ -436,21 +429,36 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
       active = false;
       continue;
     }
-    for (int c = i + 1 + tid; c < fjb; c += blockDim.x) {
-      const double w = s_row[c] + sm.scal * sm.red[c - i];
-      sm.tw[c] = sm.tau * w;
+    if (sm.tau_zero) {
+      if (tid == 0) {
+        sm.tau = 0.0;
+        if (g == 0) p.tau[i] = 0.0;
+      }
+    } else if (tid == 0) {
+      const double beta = sm.beta, rb = 1.0 / beta;
+      const double tau = (beta - s_row[i]) * rb;
+      sm.rbeta = rb;
+      sm.tau = tau;
+      if (g == 0) p.tau[i] = tau;
+    } else if (tid == 32) {
+      sm.scal = 1.0 / (s_row[i] - sm.beta);
+    }
+    __syncthreads();
+    double* x = S + (size_t)i * LS;
+    if (!sm.tau_zero) {
+      if (tid < 64) {
+        for (int c = i + 1 + tid; c < fjb; c += 64) sm.tw[c] = fma(sm.tau, s_row[c], -sm.rbeta * sm.red[c - i]);
+      } else {
+        int rr0 = i + 1 - grow0;
+        if (rr0 < 0) rr0 = 0;
+        for (int rr = rr0 + tid - 64; rr < nr; rr += (int)blockDim.x - 64) x[rr] *= sm.scal;
+      }
     }
     __syncthreads();
     PPH(4);
     // 5. apply H(i) to this CTA's rows, then the partials of column i+1
     if (!sm.tau_zero) {
-      const double scal = sm.scal;
       const int ncol_r = fjb - i - 1;
-      int rr0 = i + 1 - grow0;
-      if (rr0 < 0) rr0 = 0;
-      double* x = S + (size_t)i * LS;
-      for (int rr = rr0 + tid; rr < nr; rr += blockDim.x) x[rr] *= scal;
-      __syncthreads();
       // flattened (column, row) index over all threads, advanced by a
       // precomputed step instead of a division per entry
       if (nr > 0) {
@@ -520,8 +528,8 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
 }
 
 // Launch the clustered panel (cooperative + cluster attributes) on G CTAs
-// (a multiple of kPanelCluster); returns the CUDA error of the launch.
-cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, size_t smem, cudaStream_t s) {
+// in clusters of cs (G a multiple of cs); returns the CUDA error of the launch.
+cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, int cs, size_t smem, cudaStream_t s) {
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3(G);
   cfg.blockDim = dim3(256);
@@ -529,7 +537,7 @@ cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, size_t smem, cudaSt
   cfg.stream = s;
   cudaLaunchAttribute at[2];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kPanelCluster;
+  at[0].val.clusterDim.x = cs;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   at[1].id = cudaLaunchAttributeCooperative;
@@ -539,16 +547,16 @@ cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, size_t smem, cudaSt
   return cudaLaunchKernelEx(&cfg, k_panel_cluster, pa);
 }
 
-// Largest number of co-resident clusters for the clustered panel with the
-// given dynamic shared memory (0 if the configuration cannot run).
-int panel_cluster_capacity(size_t smem) {
+// Largest number of co-resident clusters of cs CTAs for the clustered panel
+// with the given dynamic shared memory (0 if the configuration cannot run).
+int panel_cluster_capacity(size_t smem, int cs) {
   cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(kPanelCluster);
+  cfg.gridDim = dim3(cs);
   cfg.blockDim = dim3(256);
   cfg.dynamicSmemBytes = smem;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = kPanelCluster;
+  at[0].val.clusterDim.x = cs;
   at[0].val.clusterDim.y = 1;
   at[0].val.clusterDim.z = 1;
   cfg.attrs = at;
