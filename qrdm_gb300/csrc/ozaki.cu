@@ -172,9 +172,12 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 }
 
 // ------------------------------------------------------------- GEMM 1
-// Partial W^T tile: 128 columns of C x the k (<= 64) reflector columns,
-// over the 256-row chunks [chunk_begin, chunk_end) of the window.
-// Wp[split][c][a] (FP64).  C columns start at window column st->fjb.
+// Partial W^T tiles: 128 columns of C x the k (<= 64) reflector columns,
+// summed over 256-row chunks of the window.  Persistent: the work items
+// are (column tile, chunk) pairs in tile-major order, and CTA b takes the
+// contiguous range [b per, (b + 1) per), so every CTA does the same number
+// of chunks (no partial last wave).  A CTA writes one partial per column
+// tile it touches, at Wp[b][t - (first tile of b)][128][64] (oz_wp_slot).
 //
 // Warp-specialised pipeline per 64-row block.  Sixteen converter warps
 // turn C from FP64 into its digits (the A operand), half a block (32 rows =
@@ -185,18 +188,23 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 // the V digits (B operand) of the next block arriving by bulk copy into the
 // second of two buffers.  After the last block of a 256-row chunk the
 // converter warps drain the levels into their integer accumulators (16
-// reflector columns each) and release the TMEM to the next chunk.
+// reflector columns each) and release the TMEM to the next chunk; after the
+// last chunk of a column tile they write the tile's partial.
 struct OzG1Args {
   const double* W0;     // window origin A(j, j)
   long long lda;
   int mloc, ncols;      // window rows / columns
   const double* nrm;    // partial norms, window-relative
   const unsigned char* vb1;
-  int chunks_per_split;
-  double* Wp;           // [split][npad][64]
-  int npad;
+  double* Wp;           // partials, oz_wp_slot layout
   BlockState* st;
+  int nchunk, per, mt;  // chunks per tile, items per CTA, tile slots per CTA
 };
+
+// Offset (doubles) of CTA b's partial of column tile t.
+__device__ __forceinline__ size_t oz_wp_slot(int b, int t, int nchunk, int per, int mt) {
+  return ((size_t)b * mt + (t - (b * per) / nchunk)) * (128 * 64);
+}
 
 constexpr int OZ_G1_CONV = 16;                         // converter warps
 constexpr int OZ_G1_THREADS = 32 * (OZ_G1_CONV + 1);  // + 1 MMA warp
@@ -212,20 +220,15 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   constexpr uint32_t BBYTES = S * 8192;
   __shared__ uint64_t afull[2], aempty[2], bfull[2], dready, dfree;
   __shared__ uint32_t s_tmem;
-  __shared__ int s_e[128];
   const int fjb = g.st->fjb;
   const int k = g.st->fjb_cmp;
-  const int c0 = fjb + blockIdx.x * 128;  // first window column of this tile
-  if (c0 >= g.ncols || k <= 0) return;
-  const int nchunk = ceil_div(g.mloc, 256);
-  const int ch_begin = blockIdx.y * g.chunks_per_split;
-  const int ch_end = min(nchunk, ch_begin + g.chunks_per_split);
-  const int nblk = 4 * max(0, ch_end - ch_begin);
+  const int ctiles = ceil_div(g.ncols - fjb, 128);
+  const int items = ctiles * g.nchunk;
+  const int it0 = blockIdx.x * g.per;
+  const int it1 = min(items, it0 + g.per);
+  if (it0 >= it1 || k <= 0) return;
+  const int nblk = 4 * (it1 - it0);
   const int tid = threadIdx.x, w = tid >> 5, lane = tid & 31;
-  if (tid < 128) {
-    const int c = c0 + tid;
-    s_e[tid] = c < g.ncols ? scale_exp_of(g.nrm[c]) : 0;
-  }
   if (tid == 0) {
     for (int h = 0; h < 2; ++h) {
       tc::mbar_init(&afull[h], OZ_G1_CONV);
@@ -244,9 +247,14 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   bool fail = false;
   if (w == OZ_G1_CONV) {
     // ---------------- MMA issuer and V-digit producer (one lane)
-    if (lane == 0 && nblk > 0) {
+    if (lane == 0) {
+      // V digits of block ib: chunk (item % nchunk), 64-row block ib & 3
+      auto vsrc = [&](int ib) {
+        const int ch = (it0 + (ib >> 2)) % g.nchunk;
+        return g.vb1 + (size_t)(ch * 4 + (ib & 3)) * BBYTES;
+      };
       tc::mbar_arrive_expect_tx(&bfull[0], BBYTES);
-      tc::bulk_g2s(bdig, g.vb1 + (size_t)(ch_begin * 4) * BBYTES, BBYTES, &bfull[0]);
+      tc::bulk_g2s(bdig, vsrc(0), BBYTES, &bfull[0]);
       for (int ib = 0; ib < nblk; ++ib) {
         const int kb = ib & 3;
         const uint32_t bsm = tc::smem_u32(bdig + (ib & 1) * BBYTES);
@@ -263,13 +271,12 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
             if (ib >= 1 && !tc::mbar_wait(&aempty[1], (uint32_t)((ib - 1) & 1))) fail = true;
             const int nb = (ib + 1) & 1;
             tc::mbar_arrive_expect_tx(&bfull[nb], BBYTES);
-            tc::bulk_g2s(bdig + nb * BBYTES, g.vb1 + (size_t)(ch_begin * 4 + ib + 1) * BBYTES, BBYTES,
-                         &bfull[nb]);
+            tc::bulk_g2s(bdig + nb * BBYTES, vsrc(ib + 1), BBYTES, &bfull[nb]);
           }
           tc::fence_after_sync();
           if (!fail) oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, bsm, 2 * h, 2 * h + 2, kb == 0 && h == 0);
           tc::mma_commit(&aempty[h]);
-          if (h == 1 && (kb == 3 || ib == nblk - 1)) tc::mma_commit(&dready);
+          if (h == 1 && kb == 3) tc::mma_commit(&dready);
         }
       }
       // the last commits have landed before the CTA releases TMEM
@@ -277,7 +284,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
     }
   } else {
     // ---------------- converters and level drains
-    const int row = 32 * (w & 3) + lane;  // TMEM lane = tile row = C column (c0 + row)
+    const int row = 32 * (w & 3) + lane;  // TMEM lane = tile row = C column
     const int cgrp = w >> 2;              // reflector columns [CPT cgrp, CPT cgrp + CPT)
     const uint32_t taddr = tmem + ((uint32_t)(32 * (w & 3)) << 16);
     long long acc_hi[OZ_G1_CPT];
@@ -287,12 +294,14 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
       acc_hi[i] = 0;
       acc_mid[i] = 0.f;
     }
-    // C rows r0 + 32 h + [0, 32) x columns c0 + [0, 128): row pairs spread
+    // C rows r0 + 32 h + [0, 32) x the tile's 128 columns: row pairs spread
     // over the converter threads, 16 consecutive threads on one column (256
-    // contiguous bytes)
+    // contiguous bytes); column cc = (tid >> 4) + 32 u of the tile
     double2 xv[OZ_G1_PAIRS];
     auto load_half = [&](int ib, int h) {
-      const int rb = (ch_begin + (ib >> 2)) * 256 + (ib & 3) * 64 + 32 * h;
+      const int it = it0 + (ib >> 2);
+      const int c0 = fjb + (it / g.nchunk) * 128;
+      const int rb = (it % g.nchunk) * 256 + (ib & 3) * 64 + 32 * h;
 #pragma unroll
       for (int u = 0; u < OZ_G1_PAIRS; ++u) {
         const int e = tid + 32 * OZ_G1_CONV * u;
@@ -311,9 +320,26 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         xv[u] = x;
       }
     };
-    if (nblk > 0) load_half(0, 0);
+    // shifts of this thread's conversion columns for the current tile, two
+    // 16-bit fields per word (|shift| < 2^11; registers are the limit here)
+    int cur_t = -1;
+    uint32_t shp[OZ_G1_PAIRS / 2];
+    load_half(0, 0);
     for (int ib = 0; ib < nblk; ++ib) {
       const int kb = ib & 3;
+      const int it = it0 + (ib >> 2);
+      const int t = it / g.nchunk;
+      if (t != cur_t) {
+        cur_t = t;
+#pragma unroll
+        for (int u = 0; u < OZ_G1_PAIRS; u += 2) {
+          const int c = fjb + t * 128 + ((tid + 32 * OZ_G1_CONV * u) >> 4);
+          const int c2 = c + (32 * OZ_G1_CONV >> 4);
+          const int s0 = 8 * S - (c < g.ncols ? scale_exp_of(g.nrm[c]) : 0);
+          const int s1 = 8 * S - (c2 < g.ncols ? scale_exp_of(g.nrm[c2]) : 0);
+          shp[u / 2] = ((uint32_t)s0 & 0xFFFFu) | ((uint32_t)s1 << 16);
+        }
+      }
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         // the MMAs that read this half for the previous block are complete
@@ -322,7 +348,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         for (int u = 0; u < OZ_G1_PAIRS; ++u) {
           const int e = tid + 32 * OZ_G1_CONV * u;
           const int rp = e & 15, cc = e >> 4;
-          const int sh = 8 * S - s_e[cc];
+          const int sh = (u & 1) ? (int)shp[u / 2] >> 16 : (int)(short)(shp[u / 2] & 0xFFFFu);
           int d0[S], d1[S];
           balanced_digits<S>(fixed_point(xv[u].x, sh), d0);
           balanced_digits<S>(fixed_point(xv[u].y, sh), d1);
@@ -338,7 +364,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         if (h == 0) load_half(ib, 1);
         else if (ib + 1 < nblk) load_half(ib + 1, 0);
       }
-      if (kb == 3 || ib == nblk - 1) {
+      if (kb == 3) {
         // end of a 256-row chunk: drain the levels into the accumulators
         if (!tc::mbar_wait(&dready, (uint32_t)((ib >> 2) & 1))) fail = true;
         tc::fence_after_sync();
@@ -355,19 +381,25 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         tc::fence_before_sync();
         __syncwarp();
         if (lane == 0) tc::mbar_arrive(&dfree);
-      }
-    }
-    if (!fail) {
-      // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1))
-      const int c = c0 + row;
-      double* out = g.Wp + ((size_t)blockIdx.y * g.npad + (size_t)(c - fjb)) * 64;
-      if (c < g.ncols) {
-        const int e = s_e[row];
+        // last chunk of this tile in the CTA's range: write the partial
+        if ((it + 1) % g.nchunk == 0 || it + 1 == it1) {
+          const int c = fjb + t * 128 + row;
+          if (!fail && c < g.ncols) {
+            // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1))
+            const int e = scale_exp_of(g.nrm[c]);
+            double* out = g.Wp + oz_wp_slot(blockIdx.x, t, g.nchunk, g.per, g.mt) + (size_t)row * 64;
 #pragma unroll
-        for (int i = 0; i < OZ_G1_CPT; ++i) {
-          const int a = OZ_G1_CPT * cgrp + i;
-          double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
-          out[a] = a < k ? v : 0.0;
+            for (int i = 0; i < OZ_G1_CPT; ++i) {
+              const int a = OZ_G1_CPT * cgrp + i;
+              double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
+              out[a] = a < k ? v : 0.0;
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < OZ_G1_CPT; ++i) {
+            acc_hi[i] = 0;
+            acc_mid[i] = 0.f;
+          }
         }
       }
     }
@@ -386,7 +418,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
 constexpr int OZ_W2_COLS = 16;
 
 template <int S>
-__global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp, int nsplit, int npad,
+__global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp, int nchunk, int per, int mt,
                                                    const double* __restrict__ T, int ldt, int ncols,
                                                    const BlockState* __restrict__ st,
                                                    unsigned char* __restrict__ wb2, int* __restrict__ wexp) {
@@ -397,22 +429,25 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
   const int ncols_c = ncols - st->fjb;  // columns of C
   const int cbase = blockIdx.x * OZ_W2_COLS;
   if (cbase >= ncols_c || k <= 0) return;
-  const size_t sstride = (size_t)npad * 64;
 #pragma unroll 1
   for (int e = threadIdx.x; e < OZ_W2_COLS * 64; e += blockDim.x) {
     const int cc = e / 64, a = e % 64;
     double acc = 0.0;
-    if (a < k && cbase + cc < ncols_c) {
-      const double* src = Wp + (size_t)(cbase + cc) * 64 + a;
-      int q = 0;
-      for (; q + 8 <= nsplit; q += 8) {
+    const int cw = cbase + cc;
+    if (a < k && cw < ncols_c) {
+      // the GEMM 1 CTAs that covered this column's tile, in CTA order
+      const int t = cw >> 7;
+      const int b0 = (t * nchunk) / per, b1 = ((t + 1) * nchunk - 1) / per;
+      const size_t off = (size_t)(cw & 127) * 64 + a;
+      int b = b0;
+      for (; b + 8 <= b1 + 1; b += 8) {
         double v[8];
 #pragma unroll
-        for (int u = 0; u < 8; ++u) v[u] = __ldcg(src + (size_t)(q + u) * sstride);
+        for (int u = 0; u < 8; ++u) v[u] = __ldcg(Wp + oz_wp_slot(b + u, t, nchunk, per, mt) + off);
 #pragma unroll
         for (int u = 0; u < 8; ++u) acc += v[u];
       }
-      for (; q < nsplit; ++q) acc += __ldcg(src + (size_t)q * sstride);
+      for (; b <= b1; ++b) acc += __ldcg(Wp + oz_wp_slot(b, t, nchunk, per, mt) + off);
     }
     sW[cc][a] = acc;
   }
@@ -656,18 +691,27 @@ int oz_set_attributes() {
          oz_set_attributes_s<7>();
 }
 
+// Persistent GEMM 1 partition of an mloc x ncols window (ncols - 1 columns
+// of C at most): nchunk 256-row chunks per 128-column tile, per items
+// (tile, chunk) per CTA on grid CTAs, mt partial slots per CTA.
+static void oz_gemm1_split(int mloc, int ncols, int nsm, int* nchunk, int* per, int* mt, int* grid) {
+  const int ctiles = ceil_div(std::max(1, ncols - 1), 128);  // >= 1 column is selected
+  *nchunk = ceil_div(std::max(1, mloc), 256);
+  const int items = ctiles * *nchunk;
+  *per = ceil_div(items, std::max(1, std::min(nsm, items)));
+  *grid = ceil_div(items, *per);
+  *mt = (*per - 1) / *nchunk + 2;
+}
+
 template <int S>
 static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
                   const double* T, int ldt, int nsm, BlockState* st, unsigned char* va2, unsigned char* vb1,
                   unsigned char* wb2, int* wexp, double* Wp) {
   const int mpad = ceil_div(mloc, 256) * 256;
   k_oz_slice_v<S><<<mpad / 64, OZ_TPB, (size_t)S * 16384, st_>>>(W0, lda, mloc, st, va2, vb1);
-  const int ctiles = ceil_div(ncols - 1, 128);  // >= 1 column is selected
-  const int nchunk = ceil_div(mloc, 256);
-  int nsplit = std::max(1, std::min(nchunk, ceil_div(2 * nsm, ctiles)));
-  const int cps = ceil_div(nchunk, nsplit);
-  nsplit = ceil_div(nchunk, cps);
-  const int npad = ctiles * 128;
+  // GEMM 1 partition: (column tile, chunk) items, the same count per CTA
+  int nchunk, per, mt, grid;
+  oz_gemm1_split(mloc, ncols, nsm, &nchunk, &per, &mt, &grid);
   OzG1Args a1;
   a1.W0 = W0;
   a1.lda = lda;
@@ -675,12 +719,13 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
   a1.ncols = ncols;
   a1.nrm = nrm;
   a1.vb1 = vb1;
-  a1.chunks_per_split = cps;
   a1.Wp = Wp;
-  a1.npad = npad;
   a1.st = st;
-  k_oz_gemm1<S><<<dim3(ctiles, nsplit), OZ_G1_THREADS, oz_gemm1_smem(S), st_>>>(a1);
-  k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nsplit, npad, T, ldt, ncols, st, wb2, wexp);
+  a1.nchunk = nchunk;
+  a1.per = per;
+  a1.mt = mt;
+  k_oz_gemm1<S><<<grid, OZ_G1_THREADS, oz_gemm1_smem(S), st_>>>(a1);
+  k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nchunk, per, mt, T, ldt, ncols, st, wb2, wexp);
   OzG2Args a2;
   a2.W0 = W0;
   a2.lda = lda;
@@ -720,12 +765,14 @@ void oz_workspace(int m, int n, int s, int nsm, size_t* va2, size_t* vb1, size_t
   *vb1 = (size_t)ceil_div(m, 256) * 4 * s * 8192;
   *wb2 = (size_t)ceil_div(n, 32) * s * 4096;
   *wexp = sizeof(int) * (size_t)n;
-  const int ctiles = ceil_div(n, 128);
-  const int nchunk = ceil_div(m, 256);
-  int maxsplit = 1;
-  for (int ct = 1; ct <= ctiles; ++ct)
-    maxsplit = std::max(maxsplit, std::min(nchunk, ceil_div(2 * nsm, ct)) * ct);
-  *wp = sizeof(double) * (size_t)maxsplit * 128 * 64 + sizeof(double) * (size_t)ctiles * 128 * 64;
+  // GEMM 1 partials: the largest grid x mt over the windows of the run
+  size_t slots = 0;
+  for (int mloc = m, ncols = n; mloc > 0 && ncols > 1; --mloc, --ncols) {
+    int nchunk, per, mt, grid;
+    oz_gemm1_split(mloc, ncols, nsm, &nchunk, &per, &mt, &grid);
+    slots = std::max(slots, (size_t)grid * mt);
+  }
+  *wp = sizeof(double) * std::max<size_t>(slots, 1) * 128 * 64;
 }
 
 }  // namespace qrdm
