@@ -146,12 +146,18 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_buf, int, long long* h
   }
 }
 
+// GEMM 1 drain: the S levels of 8 accumulator columns (col0..col0+7) of
+// this thread's TMEM lane.  hi = sum_{L<=5} D_L 2^(8(5-L)) exactly in int64;
+// the low levels only need FP32 accuracy (they are accumulated in FP32
+// anyway), so mid = sum_{L>=6} D_L 2^(8(S+1-L)) is formed in FP32 from the
+// FP32 level values directly (no 64-bit integer conversion, which would run
+// on the FP64 pipe).
 template <int S>
-__device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long long* hi, long long* mid) {
+__device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long long* hi, float* mid) {
 #pragma unroll
   for (int i = 0; i < 8; ++i) {
     hi[i] = 0;
-    mid[i] = 0;
+    mid[i] = 0.f;
   }
 #pragma unroll
   for (int L = 2; L <= S + 1; ++L) {
@@ -164,9 +170,8 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
     tc::tmem_wait_ld();
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      long long v = (long long)f32_to_int(__uint_as_float(r[i]));
-      if (L <= 5) hi[i] += v << (8 * (5 - L));
-      else mid[i] += v << (8 * (S + 1 - L));
+      if (L <= 5) hi[i] += (long long)f32_to_int(__uint_as_float(r[i])) << (8 * (5 - L));
+      else mid[i] = fmaf(mid[i], 256.f, __uint_as_float(r[i]));
     }
   }
 }
@@ -370,12 +375,13 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         tc::fence_after_sync();
 #pragma unroll
         for (int g8 = 0; g8 < OZ_G1_CPT / 8; ++g8) {
-          long long hi[8], mid[8];
+          long long hi[8];
+          float mid[8];
           oz_levels8<S>(taddr, OZ_G1_CPT * cgrp + 8 * g8, hi, mid);
 #pragma unroll
           for (int i = 0; i < 8; ++i) {
             acc_hi[8 * g8 + i] += hi[i];
-            acc_mid[8 * g8 + i] += (float)mid[i];
+            acc_mid[8 * g8 + i] += mid[i];
           }
         }
         tc::fence_before_sync();
