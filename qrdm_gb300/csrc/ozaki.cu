@@ -120,7 +120,13 @@ __device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32
 // Load the S levels of 8 accumulator columns (col0..col0+7) of this thread's
 // TMEM lane and combine them: hi = sum_{L<=5} D_L 2^(8(5-L)) (exact int64),
 // mid = sum_{L>=6} D_L 2^(8(S+1-L)) (int64 of exact or nearly exact values).
-// GEMM2 layout: level L at columns (L - 2) * 32 + col of one 256-column buffer
+// GEMM2 layout: level L at columns (L - 2) * 32 + col of one 256-column buffer.
+// With K <= 64 the levels L <= 5 (at most 4 digit pairs) are integers of
+// magnitude <= 4 * 64 * 2^14 = 2^22, converted exactly by adding 1.5 * 2^23
+// in FP32 (the integer lands in the low mantissa bits); the others use the
+// FP32 -> int32 conversion.
+__device__ __forceinline__ int f32_small_int(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
+
 template <int S>
 __device__ __forceinline__ void oz_levels8(uint32_t taddr_buf, int, long long* hi, long long* mid, uint32_t col) {
 #pragma unroll
@@ -139,11 +145,29 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_buf, int, long long* h
     tc::tmem_wait_ld();
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-      long long v = (long long)f32_to_int(__uint_as_float(r[i]));
-      if (L <= 5) hi[i] += v << (8 * (5 - L));
-      else mid[i] += v << (8 * (S + 1 - L));
+      if (L <= 5) hi[i] += (long long)f32_small_int(__uint_as_float(r[i])) << (8 * (5 - L));
+      else mid[i] += (long long)f32_to_int(__uint_as_float(r[i])) << (8 * (S + 1 - L));
     }
   }
+}
+
+// v 2^e rounded to nearest (ties to even), |v| < 2^62, built with integer
+// instructions (a 64-bit integer conversion runs on the FP64 pipe, the
+// scarce unit of the GEMM 2 epilogue); scales whose result would leave the
+// normal range take the conversion.
+__device__ __forceinline__ double oz_i64_scaled(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
+  unsigned long long m = (unsigned long long)(v < 0 ? -v : v);
+  const int lz = __clzll((long long)m);
+  const int ex = 1023 + 63 - lz + e;
+  if (ex <= 0 || ex >= 2046) return (double)v * pow2d(e);
+  m <<= lz;  // leading one at bit 63
+  const unsigned long long rest = m & 0x7FFull;
+  unsigned long long mant = m >> 11;  // 53 bits
+  mant += (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  // mant = 2^53 after rounding carries into the exponent field
+  return __longlong_as_double((long long)(sgn | (((unsigned long long)ex << 52) + mant - (1ull << 52))));
 }
 
 // GEMM 1 drain: the S levels of 8 accumulator columns (col0..col0+7) of
@@ -654,12 +678,12 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
             if (c < g.ncols) {
               // U = 2^e (hi 256^-5 + mid 256^-(S+1)) = comb 2^(e-57): hi < 2^45
               // and mid < 2^40, so hi 2^17 + mid 2^(57-8S) fits in 62 bits and
-              // keeps ~2^-62 of U; the power-of-two scale is exact, so one FMA
-              // rounds once, as a multiply and a subtraction would
+              // keeps ~2^-62 of U; U is rounded to FP64 once (integer
+              // instructions) and subtracted with the one FP64 operation
               const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
               constexpr int msh = 8 * (S + 1) - 40 - 17;
               const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
-              const double res = fma(-(double)comb, pow2d(e - 57), cv[jb + j]);
+              const double res = cv[jb + j] - oz_i64_scaled(comb, e - 57);
               g.W0[(size_t)c * g.lda + r] = res;
             }
           }
