@@ -335,9 +335,8 @@ def run_ours(args):
         pcy = (C.c_ulonglong * 8)()
         L.qrdm_panel_phase_cycles(pcy, 8)
         if pcy[7]:
-            pnames = ["cluster_sync", "cluster_sum", "grid_barrier", "cross_sum", "scalars",
-                      "apply", "partials"]
-            phase["panel_cta0_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames)}
+            pnames = ["block_sync", None, "grid_barrier", "totals", "scalars", "apply", "partials"]
+            phase["panel_cta0_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames) if nm}
         nblk = int(sti.nblocks)
         if prec == 0:
             # FP64 FMA GEMMs: no measured FP64 peak exists for this machine;

@@ -133,10 +133,11 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
  * lifetime.  Instrumentation only (no counterpart in the reference). */
 int qrdm_batched_phase_cycles(unsigned long long* out, int nout);
 
-/* Clustered-panel phase cycles of CTA 0 summed over the panels of the last
- * DM-QR call made with stats.timing = 1: out[0..7] = cluster barrier,
- * cluster reduction, grid barrier, cross-cluster sum, reflector scalars,
- * reflector application, next-column partials, kernel lifetime.
+/* Panel phase cycles of CTA 0 summed over the panels of the last DM-QR call
+ * made with stats.timing = 1: out[0..7] = block barrier before the grid
+ * arrival, 0 (unused), grid barrier, reading the column totals, reflector
+ * scalars, reflector application, next-column partials and their
+ * additions, kernel lifetime.
  * Instrumentation only (no counterpart in the reference). */
 int qrdm_panel_phase_cycles(unsigned long long* out, int nout);
 

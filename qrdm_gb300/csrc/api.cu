@@ -62,7 +62,7 @@ static int ctx_get(Ctx** out) {
 int set_kernel_attributes(int big) {
   {
     CK(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
-    CK(cudaFuncSetAttribute(k_panel_cluster, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
+    CK(cudaFuncSetAttribute(k_panel_red, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
     CK(cudaFuncSetAttribute(k_topk_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkTile * (int)sizeof(Cand)));
     CK(cudaFuncSetAttribute(k_dm_pick, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_permute_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
@@ -152,8 +152,9 @@ DmqrWorkspaceSizes dmqr_workspace_sizes(int m, int n, int nb, int nsm) {
   w.gram = sizeof(double) * (size_t)KM * KM;
   w.perm = sizeof(int2) * (size_t)(2 * (2 * kcap + 2));
   w.st = sizeof(BlockState);
-  const int gmax = ceil_div(panel_ctas(m, nsm), kPanelClusterSize) * kPanelClusterSize;
-  w.pan_part = sizeof(double) * 2 * (size_t)gmax * (QRDM_NB_MAX + 1);
+  const int gmax = panel_ctas(m, nsm);
+  // k_panel partials [2][G][NB_MAX+1] or k_panel_red limb totals (3 NB_MAX (NB_MAX+1)/2)
+  w.pan_part = sizeof(double) * std::max<size_t>(2 * (size_t)gmax * (QRDM_NB_MAX + 1), 3 * (size_t)QRDM_NB_MAX * (QRDM_NB_MAX + 1) / 2);
   w.pan_row = sizeof(double) * 2 * (QRDM_NB_MAX + 2);
   w.pan_bar = sizeof(unsigned) * 4;
   w.vtv_part = sizeof(double) * (size_t)gmax * QRDM_NB_MAX * QRDM_NB_MAX;
@@ -240,65 +241,37 @@ static int form_t_stored(Ctx& c, cudaStream_t s, const double* V, long long ldv,
 static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, double* d_tau,
                          int* hj, int* err);
 
-// Shapes of the clustered panel on this device.  The dynamic shared memory
-// is raised past half of an SM's, so no SM ever holds two panel CTAs (with
-// smaller requests the scheduler packs clusters two CTAs to an SM inside a
-// GPC, doubling the FP64 work on those SMs); then the co-resident cluster
-// count is recorded for clusters of 1, 2, 4 and 8 CTAs.  QRDM_PANEL_CLUSTER
-// = 1, 2, 4 or 8 pins the cluster size (tuning).
-static void choose_panel_clusters(Ctx& c) {
-  int per_sm = 0;
-  if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.dev) != cudaSuccess)
-    per_sm = 0;
-  size_t floor_b = (size_t)per_sm / 2 + 1024;
-  if (floor_b + 8192 > c.smem_optin) floor_b = 0;
-  c.pan_smem_floor = std::max<size_t>(floor_b, 1);
-  for (int ci = 0; ci < 4; ++ci) c.pan_cap[ci] = panel_cluster_capacity(c.pan_smem_floor, 1 << ci);
-  const char* f = getenv("QRDM_PANEL_CLUSTER");
-  const int v = f ? atoi(f) : 0;
-  c.pan_cs_force = (v == 1 || v == 2 || v == 4 || v == 8) ? v : 0;
-}
-
-// Launch the Householder panel on the window of pa: the clustered kernel
-// when the device can co-schedule enough 8-CTA clusters, else the plain
-// cooperative kernel.  *G_used receives the number of CTAs (the count of
-// V^T V partials).
+// Launch the Householder panel on the window of pa: the integer-total
+// kernel (one CTA per SM: its dynamic shared memory is raised past half of
+// an SM's, since the scheduler would otherwise pack two CTAs onto some SMs
+// and double their FP64 work), else the plain cooperative kernel.
+// *G_used receives the number of CTAs (the count of V^T V partials).
 static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t s, int* G_used) {
-  if (c.pan_smem_floor == 0) choose_panel_clusters(c);
-  const int g0 = panel_ctas(mloc, c.nsm);
-  // The panel's critical path is the FP64 work of one CTA per column: its
-  // rows' update and partial dot products (2 R per slot) plus the
-  // fixed-order sum of the ncl cluster totals (ncl per slot) that every CTA
-  // repeats.  Take the cluster size with the least of it among the shapes
-  // that fit one CTA per SM.
-  int best_cs = 0, best_G = 0;
-  long long best_cost = 0;
-  for (int ci = 0; ci < 4; ++ci) {
-    const int cs = 1 << ci;
-    if (c.pan_cs_force && cs != c.pan_cs_force) continue;
-    const int ncl = std::min(ceil_div(g0, cs), c.pan_cap[ci]);
-    if (ncl <= 0) continue;
-    const int G = ncl * cs, R = ceil_div(mloc, G);
-    const size_t need = (size_t)(R | 1) * kmax * sizeof(double);  // odd slab stride
-    if (need + 8192 > c.smem_optin) continue;
-    const long long cost = 2ll * R + ncl;
-    if (best_cs == 0 || cost < best_cost || (cost == best_cost && cs > best_cs)) {
-      best_cs = cs;
-      best_G = G;
-      best_cost = cost;
-    }
+  if (c.pan_smem_floor == 0) {
+    int per_sm = 0;
+    if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.dev) != cudaSuccess)
+      per_sm = 0;
+    size_t floor_b = (size_t)per_sm / 2 + 1024;
+    if (floor_b + 8192 > c.smem_optin) floor_b = 1;
+    c.pan_smem_floor = floor_b;
   }
-  if (best_cs > 0) {
-    const int G = best_G, R = ceil_div(mloc, G);
-    const size_t smem = std::max((size_t)(R | 1) * kmax * sizeof(double), c.pan_smem_floor);
-    pa.rows_per_cta = R;
-    CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
-    if (launch_panel_cluster(pa, G, best_cs, smem, s) == cudaSuccess) {
-      ++g_launches;
-      *G_used = G;
-      return 0;
+  {
+    const int G = panel_ctas(mloc, c.nsm), R = ceil_div(mloc, G);
+    const size_t need = (size_t)(R | 1) * kmax * sizeof(double);  // odd slab stride
+    const size_t smem = std::max(need, c.pan_smem_floor);
+    if (need + 8192 <= c.smem_optin && panel_red_per_sm(smem) >= 1) {
+      pa.rows_per_cta = R;
+      // the limb totals of every panel column (3 per slot, kmax (kmax + 1) / 2
+      // slots at most) and the barrier counter start at zero
+      CK(cudaMemsetAsync(pa.part, 0, sizeof(unsigned long long) * 3 * (size_t)kmax * (kmax + 1) / 2, s));
+      CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
+      if (launch_panel_red(pa, G, smem, s) == cudaSuccess) {
+        ++g_launches;
+        *G_used = G;
+        return 0;
+      }
+      cudaGetLastError();  // clear, fall back below
     }
-    cudaGetLastError();  // clear, fall back below
   }
   int G = 1, R = 1;
   size_t psmem = 0;
@@ -638,11 +611,11 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
   cudaStream_t s = c.stream();
   const int k = std::min(m, n);
   const int nbq = 64;
-  const int gmax = ceil_div(panel_ctas(m, c.nsm), kPanelClusterSize) * kPanelClusterSize;
+  const int gmax = panel_ctas(m, c.nsm);
   const int nbn = std::min(nbq, k);  // column norms of one panel
   CK(c.nrm.ensure(sizeof(double) * 2 * nbn));
   CK(c.st.ensure(sizeof(BlockState)));
-  CK(c.pan_part.ensure(sizeof(double) * 2 * (size_t)gmax * (QRDM_NB_MAX + 1)));
+  CK(c.pan_part.ensure(sizeof(double) * std::max<size_t>(2 * (size_t)gmax * (QRDM_NB_MAX + 1), 3 * (size_t)QRDM_NB_MAX * (QRDM_NB_MAX + 1) / 2)));
   CK(c.pan_row.ensure(sizeof(double) * 2 * (QRDM_NB_MAX + 2)));
   CK(c.pan_bar.ensure(sizeof(unsigned) * 4));
   CK(c.vtv_part.ensure(sizeof(double) * (size_t)gmax * QRDM_NB_MAX * QRDM_NB_MAX));
@@ -682,6 +655,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
   }
   RET(read_state(c, s));
   if (c.h_st->err & QRDM_EDEV_BARRIER_TIMEOUT) return QRDM_ERR_TIMEOUT;
+  if (c.h_st->err) return QRDM_ERR_INTERNAL;
   return 0;
 }
 

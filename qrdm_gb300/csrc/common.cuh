@@ -12,6 +12,7 @@ enum : int {
   QRDM_EDEV_BARRIER_TIMEOUT = 1,  // a bounded grid-barrier spin gave up
   QRDM_EDEV_SMEM = 2,             // a size exceeded a kernel's smem plan
   QRDM_EDEV_SWAPS = 4,            // swap list overflow
+  QRDM_EDEV_PANEL_RANGE = 8,      // a panel partial sum outside its limb range
 };
 
 // Per-block control state shared by the kernels of one DM block (device).

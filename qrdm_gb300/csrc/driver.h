@@ -53,12 +53,9 @@ struct Ctx {
   Buf qF, qg, qpart, qst;
   Buf oz_va2, oz_vb1, oz_wb2, oz_wexp, oz_wp;  // mixed-precision trailing update
   Buf b_meta, b_ws, b_prof;                     // batched DM-QR
-  Buf pan_prof;                                 // clustered panel phase cycles (timing runs)
-  // clustered panel: dynamic shared memory that keeps one CTA per SM, and
-  // the co-resident cluster count at that size for clusters of 1, 2, 4, 8
+  Buf pan_prof;                                 // panel phase cycles (timing runs)
+  // panel: dynamic shared memory that keeps one CTA per SM (0: not set)
   size_t pan_smem_floor = 0;
-  int pan_cap[4] = {0, 0, 0, 0};
-  int pan_cs_force = 0;                         // QRDM_PANEL_CLUSTER (0: by cost)
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch
   int b_grid = 0;                               // CTAs of the last batched launch
   int b_err_off = 0;                            // int offset of its error word in b_meta

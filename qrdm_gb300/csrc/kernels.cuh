@@ -23,13 +23,14 @@ struct PanelArgs {
   double* tau;        // tau + j
   const double* nrm;  // partial norms of the window columns (nrm + j)
   BlockState* st;     // reads fjb, writes fjb_cmp
-  double* part;       // [2][G][NB_MAX+1]
+  double* part;       // k_panel: [2][G][NB_MAX+1] partials; k_panel_red: limb totals
+                      // (3 per slot, fjb (fjb + 1) / 2 slots), zero at launch
   double* rowbuf;     // [2][NB_MAX+2]
   unsigned* bar;      // grid-barrier counter, zero at launch
   double* vtv_part;   // [G][NB_MAX][NB_MAX]
   int rows_per_cta;
   int allow_exit;     // 1: DM early exit (dgeqr2_mia); 0: plain dgeqr2
-  unsigned long long* prof;  // clustered panel: CTA 0's per-phase cycles [8] (added to), or null
+  unsigned long long* prof;  // k_panel_red: CTA 0's per-phase cycles [8] (added to), or null
 };
 
 struct TrailArgs {
@@ -85,10 +86,9 @@ __global__ void k_block_init(BlockState* st, int fjb, int fjb_cmp);
 __global__ void k_vtv_stored(const double* V, long long ldv, int mloc, int rows_per_chunk,
                              const BlockState* st, double* vtv_part);
 __global__ void k_panel(PanelArgs p);
-__global__ void k_panel_cluster(PanelArgs p);
-cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, int cs, size_t smem, cudaStream_t s);
-int panel_cluster_capacity(size_t smem, int cs);
-constexpr int kPanelClusterSize = 8;  // largest panel cluster (1, 2, 4 or 8 CTAs)
+__global__ void k_panel_red(PanelArgs p);
+cudaError_t launch_panel_red(const PanelArgs& pa, int G, size_t smem, cudaStream_t s);
+int panel_red_per_sm(size_t smem);
 __global__ void k_vtv_reduce(const double* vtv_part, int G, const BlockState* st, double* vtv);
 __global__ void k_larft(const double* vtv, const double* tau, const BlockState* st, double* T,
                         int ldt);

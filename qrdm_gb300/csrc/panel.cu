@@ -25,6 +25,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "ozaki_digits.cuh"
 
 namespace cg = cooperative_groups;
 
@@ -218,16 +219,86 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
   if (g == 0 && threadIdx.x == 0) p.st->fjb_cmp = kc;
 }
 
-// Partials for the clustered panel: four threads per slot, each summing
-// every fourth row of this CTA's slab in two interleaved chains, combined
-// by a fixed shuffle tree.  Slots across threads (rather than rows across a
-// warp per slot) avoid a five-step FP64 shuffle reduction per slot, and four
-// threads per slot spread the FP64 instructions over all four SM
-// sub-partitions (one warp reaches a quarter of an SM's FP64 rate).
-// Columns are LS (odd) doubles apart, so the loads of different slots fall
-// in distinct banks.
-__device__ __forceinline__ void panel_partials_slots(const double* __restrict__ S, int LS, int nr, int grow0,
-                                                    int i, int fjb, double* __restrict__ out) {
+// Exact, order-independent sums of FP64 values across CTAs: a value is
+// written as three signed 64-bit limbs of 42 bits, L0 2^-122 + L1 2^-80 +
+// L2 2^-38 (the top limb unmasked, so |v| < 2^16), each added with red.add.
+// Every FP64 value in [2^-69, 2^16) is represented exactly (its 53 bits fall
+// inside the limbs); smaller ones lose what lies below 2^-122.  Integer
+// additions do not round, so the totals are the exact sums whatever the
+// order of arrival; up to 2^20 values per total keep every limb below 2^63.
+constexpr int kLimbBits = 42;
+constexpr int kLimbBase = 122;  // weight of limb 0: 2^-122
+constexpr int kLimbs = 3;
+
+__device__ __forceinline__ void limbs_add(double v, unsigned long long* acc) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(v);
+  const int E = (int)((b >> 52) & 0x7FF);
+  unsigned long long M = b & 0xFFFFFFFFFFFFFull;
+  int s;
+  if (E == 0) {
+    s = -1074 + kLimbBase;
+  } else {
+    M |= 1ull << 52;
+    s = E - 1075 + kLimbBase;
+  }
+  const unsigned long long mask = (1ull << kLimbBits) - 1ull;
+  const bool neg = (b >> 63) != 0;
+#pragma unroll
+  for (int k = 0; k < kLimbs; ++k) {
+    const int t = s - kLimbBits * k;  // left shift of M into limb k
+    unsigned long long u;
+    if (k == kLimbs - 1) u = t >= 0 ? (t < 11 ? M << t : 0ull) : (t > -64 ? M >> -t : 0ull);
+    else if (t >= kLimbBits || t <= -64) u = 0ull;
+    else u = (t >= 0 ? (M << t) : (M >> -t)) & mask;
+    if (u) atomicAdd(acc + k, neg ? (unsigned long long)(-(long long)u) : u);
+  }
+}
+
+// The FP64 value of three limb totals: carries are propagated in integer
+// arithmetic (low limbs into [0, 2^42)), a negative total is negated limb
+// by limb and renormalised, and the three nonnegative limbs (each exact in
+// FP64) are summed, so the result is the exact total rounded (<= 2 ulp).
+__device__ __forceinline__ double limbs_value(const unsigned long long* acc) {
+  long long t0 = (long long)__ldcg(acc), t1 = (long long)__ldcg(acc + 1), t2 = (long long)__ldcg(acc + 2);
+  long long c = t0 >> kLimbBits;
+  t0 -= c << kLimbBits;
+  t1 += c;
+  c = t1 >> kLimbBits;
+  t1 -= c << kLimbBits;
+  t2 += c;
+  const bool neg = t2 < 0;
+  if (neg) {
+    t0 = -t0;
+    t1 = -t1;
+    t2 = -t2;
+    c = t0 >> kLimbBits;
+    t0 -= c << kLimbBits;
+    t1 += c;
+    c = t1 >> kLimbBits;
+    t1 -= c << kLimbBits;
+    t2 += c;
+  }
+  const double v = fma((double)t2, 0x1p-38, fma((double)t1, 0x1p-80, (double)t0 * 0x1p-122));
+  return neg ? -v : v;
+}
+
+// Offset (in limbs) of slot 0 of panel column i: columns hold fjb - i
+// slots each, packed.
+__device__ __forceinline__ size_t panel_acc_offset(int i, int fjb) {
+  return (size_t)kLimbs * ((size_t)i * fjb - (size_t)i * (i - 1) / 2);
+}
+
+// Partials of panel column i over this CTA's rows, added into the column's
+// limb totals (see k_panel_red): four threads per slot, each summing every
+// fourth row of the slab in two interleaved chains, combined by a fixed
+// shuffle tree.  Slots across threads (rather than rows across a warp per
+// slot) avoid a five-step FP64 shuffle reduction per slot, and four threads
+// per slot spread the FP64 instructions over all four SM sub-partitions
+// (one warp reaches a quarter of an SM's FP64 rate).  Columns are LS (odd)
+// doubles apart, so the loads of different slots fall in distinct banks.
+__device__ __forceinline__ void panel_partials_red(const double* __restrict__ S, int LS, int nr, int grow0,
+                                                   int i, int fjb, unsigned long long* __restrict__ acc,
+                                                   int* err) {
   const int nslot = fjb - i;
   int rr0 = i + 1 - grow0;  // first local row strictly below the diagonal
   if (rr0 < 0) rr0 = 0;
@@ -245,44 +316,41 @@ __device__ __forceinline__ void panel_partials_slots(const double* __restrict__ 
       }
       if (rr < nr) a0 = fma(x[rr], y[rr], a0);
     }
-    double acc = a0 + a1;
-    acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-    acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-    if (sl < nslot && part == 0) out[sl] = acc;
+    double v = a0 + a1;
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    if (sl < nslot && part == 0 && nr > 0) {
+      // |v| <= ~1 by the scaling (partial norms of power-of-two scaled
+      // columns); beyond the top limb's range it is reported instead
+      if ((abs_bits(v) >> 52) >= 1023ull + 16ull) atomicOr(err, QRDM_EDEV_PANEL_RANGE);
+      else limbs_add(v, acc + (size_t)kLimbs * sl);
+    }
   }
 }
 
-// ------------------------------------------------ clustered panel (K-panel)
-// Same arithmetic as k_panel, launched as clusters of 1, 2, 4 or 8 CTAs:
-// per column, each CTA's partial slots are summed by its cluster leader
-// through distributed shared memory (fixed order), the leaders publish
-// cluster totals and advance a global counter, every CTA spins (bounded) on
-// that counter and then sums the nclusters totals in a fixed order, so all
-// CTAs hold bit-identical scalars.  The w_c of the reflector application are
-// formed by one thread per column.
-constexpr int kPanelCluster = kPanelClusterSize;
-constexpr int kCrossLoads = 10;  // cluster totals in flight per thread (4 threads per slot)
-
-__global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
+// ------------------------------------------- K-panel with integer totals
+// Same arithmetic as k_panel, one CTA per SM, ONE grid barrier per panel
+// column and no cluster level.  Before the barrier every CTA adds its
+// partial slots (the sum of squares of x = A(i+1:, i) and the dot products
+// of x with the later panel columns, over its rows) into the column's limb
+// totals in global memory (limbs_add: exact integer red.add); after it every
+// CTA reads the same totals, so all CTAs hold identical scalars without a
+// fixed-order reduction, and the totals are the exact sums of the FP64
+// partials (finer than any FP64 summation).  The totals (kLimbs per slot,
+// columns packed) and the barrier counter are zeroed before the launch.
+__global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   double* S = reinterpret_cast<double*>(smem_raw);  // [fjb][LS]
   __shared__ PanelSmem sm;
-  __shared__ double s_part[2][QRDM_NB_MAX + 1];
   __shared__ double s_row[QRDM_NB_MAX];
-  cg::cluster_group cl = cg::this_cluster();
-  // cluster shape as launched (the DSMEM reads below only address ranks
-  // that exist, whatever cluster size the kernel actually runs with)
-  const unsigned crank = cl.block_rank();
-  const int csize = (int)cl.num_blocks();
   const int G = gridDim.x, g = blockIdx.x, R = p.rows_per_cta;
   const int LS = R | 1;  // column stride of the slab (odd: conflict-free per-slot loads)
-  const int ncl = G / csize, cid = g / csize;
   const int fjb = p.st->fjb;
   const int grow0 = g * R;
   const int nr = max(0, min(R, p.mloc - grow0));
   const size_t lda = (size_t)p.lda;
   double* W0 = p.A + (size_t)p.j * lda + p.j;
-  const int stride = QRDM_NB_MAX + 1;
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(p.part);  // limb totals, packed
   const int tid = threadIdx.x;
 
   for (int c = tid; c < fjb; c += blockDim.x) {
@@ -299,17 +367,12 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     S[(size_t)c * LS + rr] = W0[(size_t)c * lda + grow0 + rr] * sm.sc[c];
   }
   __syncthreads();
-  panel_partials_slots(S, LS, nr, grow0, 0, fjb, s_part[0]);
+  panel_partials_red(S, LS, nr, grow0, 0, fjb, acc, &p.st->err);
   if (grow0 <= 0 && 0 < grow0 + nr)
     for (int c = tid; c < fjb; c += blockDim.x) p.rowbuf[c] = S[(size_t)c * LS + (0 - grow0)];
 
-  // Every CTA executes exactly fjb + 1 cluster barriers whatever happens
-  // (early exit, barrier timeout), so no CTA can wait at a cluster barrier
-  // its peers never reach; after an exit or a timeout a CTA only keeps
-  // joining the cluster barriers.
   int done = fjb;
   bool ok = true;
-  bool active = true;
   // phase clock of CTA 0 (instrumentation; p.prof null in normal runs)
   const bool prof = p.prof != nullptr && g == 0 && tid == 0;
   unsigned long long pc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
@@ -326,36 +389,16 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
   for (int i = 0; i < fjb; ++i) {
     const int buf = i & 1;
     const int nslot = fjb - i;
-    double* part = p.part + (size_t)buf * ncl * stride;
     const double* rowb = p.rowbuf + (size_t)buf * (QRDM_NB_MAX + 2);
     PPH(6);
-    cl.sync();
-    PPH(0);
-    if (!active) continue;
-    // 1. cluster: leader sums the member partials (DSMEM, fixed order; all
-    //    remote loads issued before the sum)
-    if (crank == 0) {
-      for (int sl = tid; sl < nslot; sl += blockDim.x) {
-        double v[kPanelCluster];
-#pragma unroll
-        for (int r = 0; r < kPanelCluster; ++r)
-          v[r] = r < csize ? cl.map_shared_rank(&s_part[buf][0], r)[sl] : 0.0;
-        double acc = 0.0;
-#pragma unroll
-        for (int r = 0; r < kPanelCluster; ++r)
-          if (r < csize) acc += v[r];
-        part[(size_t)cid * stride + sl] = acc;
-      }
-    }
-    // 2. grid: leaders arrive, everyone waits (bounded) for all leaders
+    // 1. grid barrier: this CTA's additions and row publication are
+    //    ordered before its arrival (block barrier, then a cumulative fence)
     __syncthreads();
-    PPH(1);
+    PPH(0);
     if (tid == 0) {
-      if (crank == 0) {
-        __threadfence();
-        red_release_add_u32(p.bar, 1u);
-      }
-      const unsigned target = (unsigned)ncl * (unsigned)(i + 1);
+      __threadfence();
+      red_release_add_u32(p.bar, 1u);
+      const unsigned target = (unsigned)G * (unsigned)(i + 1);
       unsigned spins = 0;
       while (ld_acquire_u32(p.bar) < target) {
         if (++spins > QRDM_SPIN_LIMIT || (*(volatile int*)&p.st->err & QRDM_EDEV_BARRIER_TIMEOUT)) {
@@ -371,36 +414,17 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     PPH(2);
     if (sm.exit_flag == 2) {
       ok = false;
-      active = false;
-      continue;
+      break;
     }
-    // 3. fixed-order sum of the cluster totals: 4 threads per slot, every
-    //    load in flight before the adds; row i of the panel (published by
-    //    its owner) fetched alongside
-    for (int c = i + tid; c < fjb; c += blockDim.x) s_row[c] = __ldcg(rowb + c);
-    for (int base = 0; base < nslot; base += 64) {
-      const int sl = base + (tid >> 2), q0 = tid & 3;
-      double acc = 0.0;
-      if (sl < nslot) {
-        for (int qb = q0; qb < ncl; qb += 4 * kCrossLoads) {
-          double v[kCrossLoads];
-#pragma unroll
-          for (int u = 0; u < kCrossLoads; ++u) {
-            const int q = qb + 4 * u;
-            v[u] = q < ncl ? __ldcg(part + (size_t)q * stride + sl) : 0.0;
-          }
-#pragma unroll
-          for (int u = 0; u < kCrossLoads; ++u)
-            if (qb + 4 * u < ncl) acc += v[u];
-        }
-      }
-      acc += __shfl_xor_sync(0xffffffffu, acc, 1);
-      acc += __shfl_xor_sync(0xffffffffu, acc, 2);
-      if (sl < nslot && q0 == 0) sm.red[sl] = acc;
+    // 2. the column's totals (identical bits in every CTA) and row i
+    {
+      const unsigned long long* tot = acc + panel_acc_offset(i, fjb);
+      for (int c = i + tid; c < fjb; c += blockDim.x) s_row[c] = __ldcg(rowb + c);
+      for (int sl = tid; sl < nslot; sl += blockDim.x) sm.red[sl] = limbs_value(tot + (size_t)kLimbs * sl);
     }
     __syncthreads();
     PPH(3);
-    // 4. dlarfg scalars.  FP64 instructions with one active lane still take
+    // 3. dlarfg scalars.  FP64 instructions with one active lane still take
     //    the SM sub-partition's FP64 pipe for a whole warp's time, so the
     //    chain is kept short and split across warps on different
     //    sub-partitions: beta first (thread 0; the exit test compares
@@ -426,8 +450,7 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     __syncthreads();
     if (sm.exit_flag == 1) {
       done = i;
-      active = false;
-      continue;
+      break;
     }
     if (sm.tau_zero) {
       if (tid == 0) {
@@ -456,7 +479,7 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     }
     __syncthreads();
     PPH(4);
-    // 5. apply H(i) to this CTA's rows, then the partials of column i+1
+    // 4. apply H(i) to this CTA's rows, then the partials of column i+1
     if (!sm.tau_zero) {
       const int ncol_r = fjb - i - 1;
       // flattened (column, row) index over all threads, advanced by a
@@ -482,15 +505,13 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     __syncthreads();
     PPH(5);
     if (i + 1 < fjb) {
-      panel_partials_slots(S, LS, nr, grow0, i + 1, fjb, s_part[buf ^ 1]);
+      panel_partials_red(S, LS, nr, grow0, i + 1, fjb, acc + panel_acc_offset(i + 1, fjb), &p.st->err);
       if (grow0 <= i + 1 && i + 1 < grow0 + nr) {
         double* rb = p.rowbuf + (size_t)(buf ^ 1) * (QRDM_NB_MAX + 2);
         for (int c = i + 1 + tid; c < fjb; c += blockDim.x) rb[c] = S[(size_t)c * LS + (i + 1 - grow0)];
       }
     }
   }
-  // keep every CTA's shared memory alive until the leader's last DSMEM read
-  cl.sync();
   if (prof) {
     pc[7] = (unsigned long long)(clock64() - tstart);
     for (int k = 0; k < 8; ++k) atomicAdd(p.prof + k, pc[k]);
@@ -514,55 +535,31 @@ __global__ void __launch_bounds__(256) k_panel_cluster(PanelArgs p) {
     int a = t - b * (b - 1) / 2;
     const double* va = S + (size_t)a * LS;
     const double* vb = S + (size_t)b * LS;
-    double acc = 0.0;
+    double acc2 = 0.0;
     int rstart = b - grow0;
     if (rstart < 0) rstart = 0;
     for (int rr = rstart; rr < nr; ++rr) {
       int grow = grow0 + rr;
       double y = (grow == b) ? 1.0 : vb[rr];
-      acc = fma(va[rr], y, acc);
+      acc2 = fma(va[rr], y, acc2);
     }
-    vp[a * QRDM_NB_MAX + b] = acc;
+    vp[a * QRDM_NB_MAX + b] = acc2;
   }
   if (g == 0 && tid == 0) p.st->fjb_cmp = kc;
 }
 
-// Launch the clustered panel (cooperative + cluster attributes) on G CTAs
-// in clusters of cs (G a multiple of cs); returns the CUDA error of the launch.
-cudaError_t launch_panel_cluster(const PanelArgs& pa, int G, int cs, size_t smem, cudaStream_t s) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(G);
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = s;
-  cudaLaunchAttribute at[2];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = cs;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  at[1].id = cudaLaunchAttributeCooperative;
-  at[1].val.cooperative = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 2;
-  return cudaLaunchKernelEx(&cfg, k_panel_cluster, pa);
+// Launch the integer-total panel (cooperative) on G CTAs; returns the CUDA
+// error of the launch.
+cudaError_t launch_panel_red(const PanelArgs& pa, int G, size_t smem, cudaStream_t s) {
+  void* args[] = {const_cast<PanelArgs*>(&pa)};
+  return cudaLaunchCooperativeKernel((void*)k_panel_red, dim3(G), dim3(256), args, smem, s);
 }
 
-// Largest number of co-resident clusters of cs CTAs for the clustered panel
-// with the given dynamic shared memory (0 if the configuration cannot run).
-int panel_cluster_capacity(size_t smem, int cs) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(cs);
-  cfg.blockDim = dim3(256);
-  cfg.dynamicSmemBytes = smem;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeClusterDimension;
-  at[0].val.clusterDim.x = cs;
-  at[0].val.clusterDim.y = 1;
-  at[0].val.clusterDim.z = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
+// CTAs of the integer-total panel that fit on one SM with this dynamic
+// shared memory (0 if it cannot run).
+int panel_red_per_sm(size_t smem) {
   int n = 0;
-  if (cudaOccupancyMaxActiveClusters(&n, k_panel_cluster, &cfg) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_panel_red, 256, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
