@@ -1,4 +1,4 @@
-// ozaki.cu -- FP64-accurate trailing update on the BF16 tensor cores.
+// ozaki.cu -- FP64-accurate trailing update on the FP16 tensor cores.
 //
 // Replaces the FP64 dlarfb (src/dgeqrdm_work.c:762-767) in the mixed
 // precision mode:   W = V^T C,  W2 = T^T W,  C -= V W2.
@@ -8,8 +8,9 @@
 // every FP64 operand x is written, relative to a power-of-two scale 2^e
 // shared along the dot-product direction, as s base-256 balanced digits
 //     x ~= 2^e * sum_{p=1..s} d_p 256^-p,   d_p integer, |d_p| <= 128,
-// each exactly representable in BF16.  A product of two matrices becomes
-// sum over digit pairs (p, q) of exact BF16 products accumulated in FP32 on
+// each exactly representable in FP16 (packed two at a time by byte permutes
+// and one half2 subtraction, digits2_f16).  A product of two matrices becomes
+// sum over digit pairs (p, q) of exact FP16 products accumulated in FP32 on
 // tcgen05; pairs with p + q > s + 1 are dropped (their weight is below
 // 256^-(s+1)).  Pairs of equal level L = p + q share one TMEM accumulator
 // (level-major columns), so one MMA with the B digits q = 1..Q stacked along
@@ -57,26 +58,30 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_slice_v(const double* __restrict_
   const int sh = 8 * S - 1;
   for (int q = threadIdx.x; q < 32 * 32; q += blockDim.x) {
     const int rp = q >> 5, ap = q & 31;  // rows 2rp, 2rp+1; reflectors 2ap, 2ap+1
-    int d[2][2][S];
+    double v[2][2];
 #pragma unroll
     for (int i = 0; i < 2; ++i)
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         const int r = r0 + 2 * rp + i, a = 2 * ap + h;
-        double v = 0.0;
-        if (r < mloc && a < k) v = r > a ? V[(size_t)a * ldv + r] : (r == a ? 1.0 : 0.0);
-        balanced_digits<S>(fixed_point(v, sh), d[i][h]);
+        v[i][h] = 0.0;
+        if (r < mloc && a < k) v[i][h] = r > a ? V[(size_t)a * ldv + r] : (r == a ? 1.0 : 0.0);
       }
 #pragma unroll
-    for (int p = 0; p < S; ++p) {
+    for (int i = 0; i < 2; ++i) {  // va2: row 2rp+i, K = reflector pair
+      uint32_t dp[S];
+      digits2_f16<S>(v[i][0], v[i][1], sh, dp);
 #pragma unroll
-      for (int i = 0; i < 2; ++i)  // va2: row 2rp+i, K = reflector pair
-        *reinterpret_cast<uint32_t*>(sa + p * 8192 + tc::sw128_offset(2 * rp + i, 2 * ap)) =
-            pack2_bf16(d[i][0][p], d[i][1][p]);
+      for (int p = 0; p < S; ++p)
+        *reinterpret_cast<uint32_t*>(sa + p * 8192 + tc::sw128_offset(2 * rp + i, 2 * ap)) = dp[p];
+    }
 #pragma unroll
-      for (int h = 0; h < 2; ++h)  // vb1: row = reflector, K = row pair
-        *reinterpret_cast<uint32_t*>(sb + p * 8192 + tc::sw128_offset(2 * ap + h, 2 * rp)) =
-            pack2_bf16(d[0][h][p], d[1][h][p]);
+    for (int h = 0; h < 2; ++h) {  // vb1: row = reflector, K = row pair
+      uint32_t dp[S];
+      digits2_f16<S>(v[0][h], v[1][h], sh, dp);
+#pragma unroll
+      for (int p = 0; p < S; ++p)
+        *reinterpret_cast<uint32_t*>(sb + p * 8192 + tc::sw128_offset(2 * ap + h, 2 * rp)) = dp[p];
     }
   }
   __syncthreads();
@@ -106,7 +111,7 @@ __device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32
 #pragma unroll
     for (int q0 = 1; q0 <= Q; q0 += 4) {
       const int nq = min(4, Q - q0 + 1);
-      const uint32_t idesc = tc::idesc_bf16_f32(128, 64 * nq);
+      const uint32_t idesc = tc::idesc_f16_f32(128, 64 * nq);
       const uint32_t dcol = (uint32_t)((p + q0 - 2) * 64);
       for (int kk = kk0; kk < kk1; ++kk) {
         uint64_t ad = tc::desc_sw128(a_tiles + (uint32_t)(p - 1) * a_stride + kk * 32);
@@ -378,13 +383,11 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
           const int e = tid + 32 * OZ_G1_CONV * u;
           const int rp = e & 15, cc = e >> 4;
           const int sh = (u & 1) ? (int)shp[u / 2] >> 16 : (int)(short)(shp[u / 2] & 0xFFFFu);
-          int d0[S], d1[S];
-          balanced_digits<S>(fixed_point(xv[u].x, sh), d0);
-          balanced_digits<S>(fixed_point(xv[u].y, sh), d1);
+          uint32_t dp[S];
+          digits2_f16<S>(xv[u].x, xv[u].y, sh, dp);
           const uint32_t off = tc::sw128_offset(cc, 32 * h + 2 * rp);
 #pragma unroll
-          for (int p = 0; p < S; ++p)
-            *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+          for (int p = 0; p < S; ++p) *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = dp[p];
         }
         tc::fence_async_smem();
         __syncwarp();
@@ -519,13 +522,11 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
   for (int e = threadIdx.x; e < OZ_W2_COLS * 32; e += blockDim.x) {
     const int cc = e / 32, ap = e % 32;
     const int sh = 8 * S - scale_exp_of(smax[cc]);
-    int d0[S], d1[S];
-    balanced_digits<S>(fixed_point(sW[cc][2 * ap], sh), d0);
-    balanced_digits<S>(fixed_point(sW[cc][2 * ap + 1], sh), d1);
+    uint32_t dp[S];
+    digits2_f16<S>(sW[cc][2 * ap], sW[cc][2 * ap + 1], sh, dp);
     const uint32_t off = tc::sw128_offset(row0 + cc, 2 * ap);
 #pragma unroll
-    for (int q = 0; q < S; ++q)
-      *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * S + q) * 4096 + off) = pack2_bf16(d0[q], d1[q]);
+    for (int q = 0; q < S; ++q) *reinterpret_cast<uint32_t*>(wb2 + ((size_t)tile * S + q) * 4096 + off) = dp[q];
   }
 }
 
@@ -624,7 +625,7 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
           const uint32_t a0 = tc::smem_u32(adig), b0 = tc::smem_u32(bring + stg * BBYTES);
 #pragma unroll
           for (int p = 1; p <= S; ++p) {
-            const uint32_t idesc = tc::idesc_bf16_f32(128, 32 * (S + 1 - p));
+            const uint32_t idesc = tc::idesc_f16_f32(128, 32 * (S + 1 - p));
 #pragma unroll
             for (int q4 = 0; q4 < 4; ++q4)
               tc::mma_bf16(acc + (uint32_t)((p - 1) * 32), tc::desc_sw128(a0 + (uint32_t)(p - 1) * 16384u + q4 * 32),

@@ -57,6 +57,44 @@ __device__ __forceinline__ uint32_t pack2_bf16(int lo, int hi) {
 __device__ __forceinline__ unsigned short bf16_bits(int d) {
   return (unsigned short)(digit_f32_bits(d) >> 16);
 }
+// FP16 digits (the single-problem Ozaki kernels; A and B of one MMA share
+// the type).  |d| <= 512 integer pair -> two FP16, exactly: 1536 + d lies in
+// [1024, 2048), where FP16's spacing is 1, so its bits are 0x6600 + d, and
+// one packed half-precision subtraction of 1536 leaves d.
+__device__ __forceinline__ uint32_t pack2_f16(int lo, int hi) {
+  const uint32_t w = ((uint32_t)(0x6600 + lo) & 0xFFFFu) | ((uint32_t)(0x6600 + hi) << 16);
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(w), "r"(0x66006600u));
+  return r;
+}
+// Lower balanced digits of two entries from their biased fixed-point words:
+// byte b (0..3) of w0 and of w1 is digit + 128.  One byte permute places
+// them in the low bytes of the two halves, one logic op makes the halves
+// 1024 + byte (bits 0x6400 | byte) and one packed subtraction of 1152 leaves
+// byte - 128: three instructions per digit pair.
+__device__ __forceinline__ uint32_t digit_pair_f16(uint32_t w0, uint32_t w1, int b) {
+  const uint32_t sel = (uint32_t)b | ((uint32_t)b << 4) | ((uint32_t)(b + 4) << 8) | ((uint32_t)(b + 4) << 12);
+  const uint32_t t = (__byte_perm(w0, w1, sel) & 0x00FF00FFu) | 0x64006400u;
+  uint32_t r;
+  asm("sub.rn.f16x2 %0, %1, %2;" : "=r"(r) : "r"(t), "r"(0x64806480u));
+  return r;
+}
+// S FP16 digit pairs of two entries (x in the low halves) at scale 2^sh:
+// out[p] for digit p (most significant first), the balanced digits of
+// balanced_digits<S>.
+template <int S>
+__device__ __forceinline__ void digits2_f16(double x, double y, int sh, uint32_t* out) {
+  const long long bias = (long long)(0x8080808080808080ull >> (8 * (9 - S)));
+  const long long G0 = fixed_point(x, sh) + bias, G1 = fixed_point(y, sh) + bias;
+  out[0] = pack2_f16((int)(G0 >> (8 * (S - 1))), (int)(G1 >> (8 * (S - 1))));
+#pragma unroll
+  for (int b = 0; b < S - 1; ++b) {  // byte b from the bottom = digit S-1-b
+    const uint32_t w0 = b < 4 ? (uint32_t)G0 : (uint32_t)((unsigned long long)G0 >> 32);
+    const uint32_t w1 = b < 4 ? (uint32_t)G1 : (uint32_t)((unsigned long long)G1 >> 32);
+    out[S - 1 - b] = digit_pair_f16(w0, w1, b & 3);
+  }
+}
+
 // exact FP32 integer (|x| < 2^31) -> int32
 __device__ __forceinline__ int f32_to_int(float x) { return __float2int_rn(x); }
 
