@@ -304,13 +304,13 @@ __device__ __forceinline__ void oz_levels16(uint32_t taddr, uint32_t col, long l
   }
 }
 
-// digit-pair MMAs of one operand pair: A digits p at a + (p-1) 16 KB, B
+// digit-pair MMAs of one operand pair (FP16 digits, digits2_f16): A digits p at a + (p-1) 16 KB, B
 // digits stacked at b (4 KB each, 32 rows), K16 steps [0, nkk); level
 // L = p + q at TMEM column (L - 2) * 32 of d
 __device__ __forceinline__ void oz_mma_block(uint32_t d, uint32_t a, uint32_t b, int nkk, bool first) {
 #pragma unroll
   for (int p = 1; p <= OZS; ++p) {
-    const uint32_t idesc = tc::idesc_bf16_f32(128, 32 * (OZS + 1 - p));
+    const uint32_t idesc = tc::idesc_f16_f32(128, 32 * (OZS + 1 - p));
     for (int kk = 0; kk < nkk; ++kk)
       tc::mma_bf16(d + (uint32_t)((p - 1) * 32), tc::desc_sw128(a + (uint32_t)(p - 1) * 16384u + kk * 32),
                    tc::desc_sw128(b + kk * 32), idesc, (first && p == 1 && kk == 0) ? 0u : 1u);
@@ -411,13 +411,12 @@ __device__ void cta_vtv_oz(OzCtx& z, const double* V0, long long lda, int mloc, 
     const int r0 = kb * 64;
     for (int e = tid; e < 32 * 32; e += 256) {
       const int a = e >> 5, kp = e & 31, r = r0 + 2 * kp;
-      int d0[OZS], d1[OZS];
-      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, a), SH_V), d0);
-      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r + 1, a), SH_V), d1);
+      uint32_t dp[OZS];
+      digits2_f16<OZS>(vval(V0, lda, mloc, kc, r, a), vval(V0, lda, mloc, kc, r + 1, a), SH_V, dp);
       const uint32_t off = tc::sw128_offset(a, 2 * kp);
 #pragma unroll
       for (int p = 0; p < OZS; ++p) {
-        const uint32_t pk = pack2_bf16(d0[p], d1[p]);
+        const uint32_t pk = dp[p];
         *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = pk;
         *reinterpret_cast<uint32_t*>(z.bdig + p * 4096 + off) = pk;
       }
@@ -488,24 +487,22 @@ __device__ void cta_trailing_oz(OzCtx& z, const double* V0, double* C0, long lon
           if (r + 1 < mloc) x1 = col[r + 1];
         }
         const int sh = 8 * OZS - z.s_e[cc];
-        int d0[OZS], d1[OZS];
-        balanced_digits<OZS>(fixed_point(x0, sh), d0);
-        balanced_digits<OZS>(fixed_point(x1, sh), d1);
+        uint32_t dp[OZS];
+        digits2_f16<OZS>(x0, x1, sh, dp);
         const uint32_t off = tc::sw128_offset(cc, 2 * rp);
 #pragma unroll
         for (int p = 0; p < OZS; ++p)
-          *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+          *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = dp[p];
       }
       // V rows r0..r0+63 x 32 reflectors -> B digits (tile row = reflector)
       for (int e = tid; e < 32 * 32; e += 256) {
         const int a = e >> 5, kp = e & 31, r = r0 + 2 * kp;
-        int d0[OZS], d1[OZS];
-        balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, a), SH_V), d0);
-        balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r + 1, a), SH_V), d1);
+        uint32_t dp[OZS];
+        digits2_f16<OZS>(vval(V0, lda, mloc, kc, r, a), vval(V0, lda, mloc, kc, r + 1, a), SH_V, dp);
         const uint32_t off = tc::sw128_offset(a, 2 * kp);
 #pragma unroll
         for (int p = 0; p < OZS; ++p)
-          *reinterpret_cast<uint32_t*>(z.bdig + p * 4096 + off) = pack2_bf16(d0[p], d1[p]);
+          *reinterpret_cast<uint32_t*>(z.bdig + p * 4096 + off) = dp[p];
       }
       tc::fence_async_smem();
       __syncthreads();
@@ -566,12 +563,11 @@ __device__ void cta_trailing_oz(OzCtx& z, const double* V0, double* C0, long lon
     for (int ap = 0; ap < 16; ++ap) {
       const double y0 = 2 * ap < kc ? W[(size_t)(2 * ap) * ldw + c] : 0.0;
       const double y1 = 2 * ap + 1 < kc ? W[(size_t)(2 * ap + 1) * ldw + c] : 0.0;
-      int d0[OZS], d1[OZS];
-      balanced_digits<OZS>(fixed_point(y0, sh), d0);
-      balanced_digits<OZS>(fixed_point(y1, sh), d1);
+      uint32_t dp[OZS];
+      digits2_f16<OZS>(y0, y1, sh, dp);
       const uint32_t off = tc::sw128_offset(c & 31, 2 * ap);
 #pragma unroll
-      for (int q = 0; q < OZS; ++q) *reinterpret_cast<uint32_t*>(tile + q * 4096 + off) = pack2_bf16(d0[q], d1[q]);
+      for (int q = 0; q < OZS; ++q) *reinterpret_cast<uint32_t*>(tile + q * 4096 + off) = dp[q];
     }
   }
   __syncthreads();
@@ -581,13 +577,12 @@ __device__ void cta_trailing_oz(OzCtx& z, const double* V0, double* C0, long lon
     // V rows r0..r0+127 x 32 reflectors -> A digits (tile row = C row)
     for (int e = tid; e < 128 * 16; e += 256) {
       const int rr = e >> 4, ap = e & 15, r = r0 + rr;
-      int d0[OZS], d1[OZS];
-      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, 2 * ap), SH_V), d0);
-      balanced_digits<OZS>(fixed_point(vval(V0, lda, mloc, kc, r, 2 * ap + 1), SH_V), d1);
+      uint32_t dp[OZS];
+      digits2_f16<OZS>(vval(V0, lda, mloc, kc, r, 2 * ap), vval(V0, lda, mloc, kc, r, 2 * ap + 1), SH_V, dp);
       const uint32_t off = tc::sw128_offset(rr, 2 * ap);
 #pragma unroll
       for (int p = 0; p < OZS; ++p)
-        *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = pack2_bf16(d0[p], d1[p]);
+        *reinterpret_cast<uint32_t*>(z.adig + p * 16384 + off) = dp[p];
     }
     for (int t = 0; t < ntile; ++t) {
       {
