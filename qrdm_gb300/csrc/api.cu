@@ -436,6 +436,9 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     PH(1);
     // ---- panel dgeqr2_mia (src/dgeqr2.c) with early exit
     int G = 1;
+    // mixed precision with a trailing matrix: T factor and update on the
+    // tensor cores (the block's V^T V from the first GEMM)
+    const bool oz_block = mixed && kmax <= 64 && nloc > 1;
     {
       PanelArgs pa;
       pa.A = P.A;
@@ -452,12 +455,15 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       pa.vtv_part = c.vtv_part.as<double>();
       pa.rows_per_cta = 1;
       pa.allow_exit = 1;
+      pa.skip_vtv = oz_block ? 1 : 0;
       pa.prof = timing ? c.pan_prof.as<unsigned long long>() : nullptr;
       RET(launch_panel(c, pa, mloc, kmax, s, &G));
     }
     PH(2);
-    // ---- T factor (dlarft 'F','C', src/dgeqrdm_work.c:751-754)
-    {
+    // ---- T factor (dlarft 'F','C', src/dgeqrdm_work.c:751-754); the mixed
+    //      path forms it inside its trailing update, from the tensor-core
+    //      V^T V, between the two GEMMs
+    if (!oz_block) {
       int npair = kmax * (kmax - 1) / 2;
       k_vtv_reduce<<<std::max(1, ceil_div(8 * npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());
       RET(check_launch());
@@ -468,11 +474,11 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     // ---- trailing update (dlarfb 'L','T','F','C', src/dgeqrdm_work.c:762-767)
     {
       double* W0 = P.A + (size_t)j * lda + j;
-      if (mixed && kmax <= 64) {
-        if (oz_trailing_update(s, W0, lda, mloc, nloc, nrm + j, c.T.as<double>(), kmax, slices, nsm, d_st,
-                               c.oz_va2.as<unsigned char>(), c.oz_vb1.as<unsigned char>(),
-                               c.oz_wb2.as<unsigned char>(), c.oz_wexp.as<int>(), c.oz_wp.as<double>(),
-                               &g_launches))
+      if (oz_block) {
+        if (oz_trailing_update(s, W0, lda, mloc, nloc, nrm + j, c.T.as<double>(), kmax, P.tau + j,
+                               c.vtv.as<double>(), slices, nsm, d_st, c.oz_va2.as<unsigned char>(),
+                               c.oz_vb1.as<unsigned char>(), c.oz_wb2.as<unsigned char>(),
+                               c.oz_wexp.as<int>(), c.oz_wp.as<double>(), &g_launches))
           return QRDM_ERR_CUDA;
       } else {
         RET(apply_block_reflector(c, s, W0, lda, W0, lda, mloc, nloc, 1, 1, kmax, d_st));
@@ -644,6 +650,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
     pa.vtv_part = c.vtv_part.as<double>();
     pa.rows_per_cta = 1;
     pa.allow_exit = 0;
+    pa.skip_vtv = 0;
     pa.prof = nullptr;
     RET(launch_panel(c, pa, mloc, kb, s, &G));
     int npair = kb * (kb - 1) / 2;

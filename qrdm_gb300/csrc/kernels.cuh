@@ -14,7 +14,7 @@ struct Cand {
 constexpr int kTopkTile = 2048;   // entries sorted per CTA by k_topk_tile
 constexpr int kTopkFinal = 4096;  // entries sorted by k_topk_final
 
-struct PanelArgs {
+struct PanelArgs {  // every field is set by the launching code
   double* A;
   long long lda;
   int j;              // window origin A(j, j)
@@ -30,6 +30,7 @@ struct PanelArgs {
   double* vtv_part;   // [G][NB_MAX][NB_MAX]
   int rows_per_cta;
   int allow_exit;     // 1: DM early exit (dgeqr2_mia); 0: plain dgeqr2
+  int skip_vtv;       // 1: leave the V^T V partials to the caller (mixed precision)
   unsigned long long* prof;  // k_panel_red: CTA 0's per-phase cycles [8] (added to), or null
 };
 
@@ -102,9 +103,13 @@ __global__ void k_trail_update(TrailArgs p);
 
 // ozaki.cu
 int oz_set_attributes();
+// Mixed-precision trailing update of one DM block, T factor included (T is
+// formed from the V^T V rows of the first GEMM; the panel leaves them out):
+// writes T (ldt = kmax) from tau and the scratch vtv, then updates C.
 int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
-                       const double* T, int ldt, int s, int nsm, BlockState* st, unsigned char* va2,
-                       unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp, int* launches);
+                       double* T, int ldt, const double* tau, double* vtv, int s, int nsm, BlockState* st,
+                       unsigned char* va2, unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp,
+                       int* launches);
 void oz_workspace(int m, int n, int s, int nsm, size_t* va2, size_t* vb1, size_t* wb2, size_t* wexp,
                   size_t* wp);
 

@@ -206,8 +206,12 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 }
 
 // ------------------------------------------------------------- GEMM 1
-// Partial W^T tiles: 128 columns of C x the k (<= 64) reflector columns,
-// summed over 256-row chunks of the window.  Persistent: the work items
+// Partial W^T tiles: 128 window columns x the k (<= 64) reflector columns,
+// summed over 256-row chunks of the window.  The window starts at the
+// block's first column: its first k columns enter as V itself (unit
+// diagonal, zeros above, scale 2^2), so their rows of W^T are V^T V, which
+// the T factor needs (columns k..fjb-1, selected but not factored, enter as
+// zeros); the trailing matrix C starts at column fjb.  Persistent: the work items
 // are (column tile, chunk) pairs in tile-major order, and CTA b takes the
 // contiguous range [b per, (b + 1) per), so every CTA does the same number
 // of chunks (no partial last wave).  A CTA writes one partial per column
@@ -240,6 +244,12 @@ __device__ __forceinline__ size_t oz_wp_slot(int b, int t, int nchunk, int per, 
   return ((size_t)b * mt + (t - (b * per) / nchunk)) * (128 * 64);
 }
 
+// Scale exponent of window column c in GEMM 1: 2 for the reflector
+// columns (|v| <= 1), the partial norm's for the columns of C.
+__device__ __forceinline__ int oz_g1_exp(const OzG1Args& g, int c, int fjb) {
+  return c < fjb ? 2 : (c < g.ncols ? scale_exp_of(g.nrm[c]) : 0);
+}
+
 constexpr int OZ_G1_CONV = 16;                         // converter warps
 constexpr int OZ_G1_THREADS = 32 * (OZ_G1_CONV + 1);  // + 1 MMA warp
 constexpr int OZ_G1_PAIRS = 2048 / (32 * OZ_G1_CONV);  // row pairs per thread per half block
@@ -256,7 +266,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   __shared__ uint32_t s_tmem;
   const int fjb = g.st->fjb;
   const int k = g.st->fjb_cmp;
-  const int ctiles = ceil_div(g.ncols - fjb, 128);
+  const int ctiles = ceil_div(g.ncols, 128);
   const int items = ctiles * g.nchunk;
   const int it0 = blockIdx.x * g.per;
   const int it1 = min(items, it0 + g.per);
@@ -334,7 +344,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
     double2 xv[OZ_G1_PAIRS];
     auto load_half = [&](int ib, int h) {
       const int it = it0 + (ib >> 2);
-      const int c0 = fjb + (it / g.nchunk) * 128;
+      const int c0 = (it / g.nchunk) * 128;
       const int rb = (it % g.nchunk) * 256 + (ib & 3) * 64 + 32 * h;
 #pragma unroll
       for (int u = 0; u < OZ_G1_PAIRS; ++u) {
@@ -342,7 +352,15 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         const int rp = e & 15, cc = e >> 4;
         const int c = c0 + cc, r = rb + 2 * rp;
         double2 x = make_double2(0.0, 0.0);
-        if (c < g.ncols) {
+        if (c < fjb) {
+          // reflector column: V (unit diagonal, zeros above); selected but
+          // unfactored columns: zero
+          if (c < k) {
+            const double* col = g.W0 + (size_t)c * g.lda;
+            x.x = r > c && r < g.mloc ? __ldg(col + r) : (r == c ? 1.0 : 0.0);
+            x.y = r + 1 > c && r + 1 < g.mloc ? __ldg(col + r + 1) : (r + 1 == c ? 1.0 : 0.0);
+          }
+        } else if (c < g.ncols) {
           const double* col = g.W0 + (size_t)c * g.lda;
           if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
             x = __ldg(reinterpret_cast<const double2*>(col + r));
@@ -367,10 +385,10 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         cur_t = t;
 #pragma unroll
         for (int u = 0; u < OZ_G1_PAIRS; u += 2) {
-          const int c = fjb + t * 128 + ((tid + 32 * OZ_G1_CONV * u) >> 4);
+          const int c = t * 128 + ((tid + 32 * OZ_G1_CONV * u) >> 4);
           const int c2 = c + (32 * OZ_G1_CONV >> 4);
-          const int s0 = 8 * S - (c < g.ncols ? scale_exp_of(g.nrm[c]) : 0);
-          const int s1 = 8 * S - (c2 < g.ncols ? scale_exp_of(g.nrm[c2]) : 0);
+          const int s0 = 8 * S - oz_g1_exp(g, c, fjb);
+          const int s1 = 8 * S - oz_g1_exp(g, c2, fjb);
           shp[u / 2] = ((uint32_t)s0 & 0xFFFFu) | ((uint32_t)s1 << 16);
         }
       }
@@ -416,10 +434,10 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
         if (lane == 0) tc::mbar_arrive(&dfree);
         // last chunk of this tile in the CTA's range: write the partial
         if ((it + 1) % g.nchunk == 0 || it + 1 == it1) {
-          const int c = fjb + t * 128 + row;
+          const int c = t * 128 + row;
           if (!fail && c < g.ncols) {
             // W^T(c, a) = 2^(e_c + 1) (hi 256^-5 + mid 256^-(S+1))
-            const int e = scale_exp_of(g.nrm[c]);
+            const int e = oz_g1_exp(g, c, fjb);
             double* out = g.Wp + oz_wp_slot(blockIdx.x, t, g.nchunk, g.per, g.mt) + (size_t)row * 64;
 #pragma unroll
             for (int i = 0; i < OZ_G1_CPT; ++i) {
@@ -441,6 +459,26 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   tc::fence_before_sync();
   __syncthreads();
   if (w == 0) tc::tmem_dealloc(tmem, 512);
+}
+
+// ------------------------------------------------------------ V^T V
+// V^T V for the T factor from the GEMM 1 partials of the reflector columns
+// (window columns 0..k-1, all in column tile 0): vtv[b(b-1)/2 + a] =
+// sum over the CTAs that covered tile 0, in CTA order, of W^T(b, a), a < b.
+__global__ void __launch_bounds__(256) k_oz_vtv(const double* __restrict__ Wp, int nchunk, int per, int mt,
+                                                const BlockState* __restrict__ st, double* __restrict__ vtv) {
+  const int k = st->fjb_cmp;
+  const int npair = k * (k - 1) / 2;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= npair) return;
+  int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+  while (b * (b - 1) / 2 > t) --b;
+  while ((b + 1) * b / 2 <= t) ++b;
+  const int a = t - b * (b - 1) / 2;
+  const int b1 = (nchunk - 1) / per;
+  double acc = 0.0;
+  for (int q = 0; q <= b1; ++q) acc += __ldcg(Wp + oz_wp_slot(q, 0, nchunk, per, mt) + (size_t)b * 64 + a);
+  vtv[t] = acc;
 }
 
 // ------------------------------------------- W2 = T^T W and its digits
@@ -468,10 +506,12 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
     double acc = 0.0;
     const int cw = cbase + cc;
     if (a < k && cw < ncols_c) {
-      // the GEMM 1 CTAs that covered this column's tile, in CTA order
-      const int t = cw >> 7;
+      // the GEMM 1 CTAs that covered this column's tile (window column
+      // fjb + cw), in CTA order
+      const int wc = st->fjb + cw;
+      const int t = wc >> 7;
       const int b0 = (t * nchunk) / per, b1 = ((t + 1) * nchunk - 1) / per;
-      const size_t off = (size_t)(cw & 127) * 64 + a;
+      const size_t off = (size_t)(wc & 127) * 64 + a;
       int b = b0;
       for (; b + 8 <= b1 + 1; b += 8) {
         double v[8];
@@ -722,11 +762,11 @@ int oz_set_attributes() {
          oz_set_attributes_s<7>();
 }
 
-// Persistent GEMM 1 partition of an mloc x ncols window (ncols - 1 columns
-// of C at most): nchunk 256-row chunks per 128-column tile, per items
-// (tile, chunk) per CTA on grid CTAs, mt partial slots per CTA.
+// Persistent GEMM 1 partition of an mloc x ncols window (all its columns:
+// the reflectors, then C): nchunk 256-row chunks per 128-column tile, per
+// items (tile, chunk) per CTA on grid CTAs, mt partial slots per CTA.
 static void oz_gemm1_split(int mloc, int ncols, int nsm, int* nchunk, int* per, int* mt, int* grid) {
-  const int ctiles = ceil_div(std::max(1, ncols - 1), 128);  // >= 1 column is selected
+  const int ctiles = ceil_div(std::max(1, ncols), 128);
   *nchunk = ceil_div(std::max(1, mloc), 256);
   const int items = ctiles * *nchunk;
   *per = ceil_div(items, std::max(1, std::min(nsm, items)));
@@ -736,8 +776,8 @@ static void oz_gemm1_split(int mloc, int ncols, int nsm, int* nchunk, int* per, 
 
 template <int S>
 static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
-                  const double* T, int ldt, int nsm, BlockState* st, unsigned char* va2, unsigned char* vb1,
-                  unsigned char* wb2, int* wexp, double* Wp) {
+                  double* T, int ldt, const double* tau, double* vtv, int nsm, BlockState* st,
+                  unsigned char* va2, unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp) {
   const int mpad = ceil_div(mloc, 256) * 256;
   k_oz_slice_v<S><<<mpad / 64, OZ_TPB, (size_t)S * 16384, st_>>>(W0, lda, mloc, st, va2, vb1);
   // GEMM 1 partition: (column tile, chunk) items, the same count per CTA
@@ -756,6 +796,9 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
   a1.per = per;
   a1.mt = mt;
   k_oz_gemm1<S><<<grid, OZ_G1_THREADS, oz_gemm1_smem(S), st_>>>(a1);
+  // T factor from the V^T V rows of W (dlarft 'F','C'), needed from here on
+  k_oz_vtv<<<ceil_div(ldt * (ldt - 1) / 2, 256) + 1, 256, 0, st_>>>(Wp, nchunk, per, mt, st, vtv);
+  launch_larft(vtv, tau, st, T, ldt, st_);
   k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nchunk, per, mt, T, ldt, ncols, st, wb2, wexp);
   OzG2Args a2;
   a2.W0 = W0;
@@ -774,18 +817,19 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
 // Whole mixed-precision trailing update of one DM block.  Buffers: va2/vb1
 // (V digits), wb2 (W2 digits), wexp (n ints), Wp (nsplit x npad x 64 FP64).
 int oz_trailing_update(cudaStream_t st_, double* W0, long long lda, int mloc, int ncols, const double* nrm,
-                       const double* T, int ldt, int s, int nsm, BlockState* st, unsigned char* va2,
-                       unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp, int* launches) {
-  if (ncols <= 1 || mloc <= 0) return 0;
+                       double* T, int ldt, const double* tau, double* vtv, int s, int nsm, BlockState* st,
+                       unsigned char* va2, unsigned char* vb1, unsigned char* wb2, int* wexp, double* Wp,
+                       int* launches) {
+  if (ncols <= 1 || mloc <= 0) return 0;  // no trailing columns: no update, no T
   int r = 1;
   switch (s) {
-    case 4: r = oz_run<4>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
-    case 5: r = oz_run<5>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
-    case 6: r = oz_run<6>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
-    case 7: r = oz_run<7>(st_, W0, lda, mloc, ncols, nrm, T, ldt, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 4: r = oz_run<4>(st_, W0, lda, mloc, ncols, nrm, T, ldt, tau, vtv, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 5: r = oz_run<5>(st_, W0, lda, mloc, ncols, nrm, T, ldt, tau, vtv, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 6: r = oz_run<6>(st_, W0, lda, mloc, ncols, nrm, T, ldt, tau, vtv, nsm, st, va2, vb1, wb2, wexp, Wp); break;
+    case 7: r = oz_run<7>(st_, W0, lda, mloc, ncols, nrm, T, ldt, tau, vtv, nsm, st, va2, vb1, wb2, wexp, Wp); break;
     default: return 1;
   }
-  if (launches) *launches += 4;
+  if (launches) *launches += 6;
   return r;
 }
 

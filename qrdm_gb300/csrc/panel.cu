@@ -197,7 +197,7 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
   // partial V^T V over this CTA's rows: vtv[a][b], a < b < kc, with the unit
   // diagonal of V(:, b) at row b and zeros above it.
   double* vp = p.vtv_part + (size_t)g * QRDM_NB_MAX * QRDM_NB_MAX;
-  int npair = kc * (kc - 1) / 2;
+  int npair = p.skip_vtv ? 0 : kc * (kc - 1) / 2;
   for (int t = threadIdx.x; t < npair; t += blockDim.x) {
     // decode t -> (a, b), b > a, pairs ordered by b then a
     int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
@@ -526,8 +526,10 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
     if (!(c < kc && grow > c)) v = v / sm.sc[c];
     W0[(size_t)c * lda + grow] = v;
   }
+  // (V^T V: FP64 partials over this CTA's rows, unless the caller forms it
+  // on the tensor cores)
   double* vp = p.vtv_part + (size_t)g * QRDM_NB_MAX * QRDM_NB_MAX;
-  int npair = kc * (kc - 1) / 2;
+  int npair = p.skip_vtv ? 0 : kc * (kc - 1) / 2;
   for (int t = tid; t < npair; t += blockDim.x) {
     int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
     while (b * (b - 1) / 2 > t) --b;
