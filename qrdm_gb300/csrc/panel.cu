@@ -647,12 +647,12 @@ __global__ void k_vtv_reduce(const double* __restrict__ vtv_part, int G,
 // Schreiber & Van Loan), so each column j of T is an independent
 // back-substitution: T(j,j) = tau_j and, for i = j-1 .. 0,
 // T(i,j) = -tau_i sum_{l=i+1..j} U(i,l) T(l,j) (row i zero when tau_i = 0,
-// as in dlarft).  One warp (one CTA) per column, the sum over l spread over
-// the lanes: the columns run on as many SMs as there are columns, and each
-// column's serial chain of j steps costs a few FP64 warp instructions per
-// step (a single warp reaches only a quarter of an SM's FP64 rate, so the
-// chain, not the flops, bounds the kernel).  V^T V is staged in shared
-// memory first (coalesced), since every step reads scattered entries.
+// as in dlarft).  One warp (one CTA) per column: the columns run on as
+// many SMs as there are columns, and each column's serial chain of j steps
+// costs a shuffle and a few FP64 warp instructions per step (a single warp
+// reaches only a quarter of an SM's FP64 rate, so the chain, not the flops,
+// bounds the kernel).  V^T V is staged in shared memory first (coalesced),
+// since every step reads scattered entries.
 __global__ void __launch_bounds__(32) k_larft(const double* __restrict__ vtv,
                                               const double* __restrict__ tau,
                                               const BlockState* __restrict__ st,
@@ -662,26 +662,49 @@ __global__ void __launch_bounds__(32) k_larft(const double* __restrict__ vtv,
   const int j = blockIdx.x;
   if (j >= k) return;
   double* sU = reinterpret_cast<double*>(smem_raw);  // packed strict upper, U(i,l) at l(l-1)/2 + i
-  double* col = sU + (size_t)k * (k - 1) / 2;        // T(0:k, j)
+  double* stau = sU + (size_t)k * (k - 1) / 2;       // tau(0:k)
   const int lane = threadIdx.x;
   const int npair = j * (j + 1) / 2;  // entries with l <= j
   for (int e = lane; e < npair; e += 32) sU[e] = vtv[e];
-  for (int i = lane; i < k; i += 32) col[i] = 0.0;
+  for (int i = lane; i < k; i += 32) stau[i] = tau[i];
   __syncwarp();
-  if (lane == 0) col[j] = tau[j];
-  __syncwarp();
-  for (int i = j - 1; i >= 0; --i) {
-    const double ti = tau[i];
-    double acc = 0.0;
-    for (int l = i + 1 + lane; l <= j; l += 32) acc = fma(sU[l * (l - 1) / 2 + i], col[l], acc);
-    acc = warp_sum(acc);
-    if (lane == 0) col[i] = ti != 0.0 ? -ti * acc : 0.0;
-    __syncwarp();
+  // Column-oriented back substitution: lane owns rows i = lane + 32 q and
+  // their running sums acc(i) = sum_{l > i, solved} U(i,l) T(l,j).  Step l
+  // takes acc(l) from its owner, solves T(l,j) = -tau_l acc(l) (tau_j on
+  // the diagonal) and adds U(i,l) T(l,j) into every acc(i), i < l: per step
+  // one shuffle and two or three FP64 instructions, no reduction tree.
+  constexpr int RPL = QRDM_NB_MAX / 32;
+  double acc[RPL], colv[RPL];
+#pragma unroll
+  for (int q = 0; q < RPL; ++q) {
+    acc[q] = 0.0;
+    colv[q] = 0.0;
   }
-  for (int i = lane; i < k; i += 32) T[(size_t)j * ldt + i] = col[i];
+  for (int l = j; l >= 0; --l) {
+    const int ql = l >> 5;
+    double mine = acc[0];
+#pragma unroll
+    for (int q = 1; q < RPL; ++q)
+      if (ql == q) mine = acc[q];
+    const double al = __shfl_sync(0xffffffffu, mine, l & 31);
+    const double tl = stau[l];
+    const double cl = l == j ? tl : (tl != 0.0 ? -tl * al : 0.0);
+#pragma unroll
+    for (int q = 0; q < RPL; ++q) {
+      const int i = lane + 32 * q;
+      if (32 * q < l) {  // warp-uniform: some row of this slot lies above l
+        if (i < l) acc[q] = fma(sU[l * (l - 1) / 2 + i], cl, acc[q]);
+      }
+      if (i == l) colv[q] = cl;
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < RPL; ++q) {
+    const int i = lane + 32 * q;
+    if (i < k) T[(size_t)j * ldt + i] = colv[q];
+  }
 }
 
-// Launch of k_larft for blocks of at most kmax reflectors.
 void launch_larft(const double* vtv, const double* tau, const BlockState* st, double* T, int kmax,
                   cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)kmax * (kmax - 1) / 2 + (size_t)kmax);
