@@ -350,26 +350,51 @@ def run_ours(args):
                     "per_launch_basis": f"4 m' n' k flops per DM block, {nblk} blocks"}
         else:
             # Ozaki split: s digits per operand, the s (s + 1) / 2 digit
-            # products of level <= s + 1 are BF16 GEMMs of the FP64 shape
+            # products of level <= s + 1 are FP16 GEMMs of the FP64 shape
+            # (FP16 and BF16 dense tensor rates are equal on this GPU: the
+            # measured BF16 GEMM peak is the denominator).  The update also
+            # streams C through HBM (GEMM 1 reads it, GEMM 2 reads and
+            # writes it: 24 algorithmic bytes per C entry and block); the
+            # bound is whichever roof takes longer for this workload.
             s_dig = int(args.slices or default_options().slices) or 7
             prods = s_dig * (s_dig + 1) // 2
             tflop = sti.trail_flops * prods
-            achieved = tflop / (sti.ms_trail / 1e3) / 1e12 if sti.ms_trail > 0 else 0.0
-            peak = peaks.get("bf16_tflops_sustained")
-            roof = {"bound": "tensor", "kernel": "Ozaki trailing update (k_oz_slice_v, "
-                    "k_oz_gemm1, k_oz_w2, k_oz_gemm2), BF16 tcgen05", "achieved": achieved,
-                    "peak": peak, "peak_kind": f"{peak_kind} bf16 sustained (the phase runs "
-                    "inside a long step)", "unit": "TFLOP/s", "frac": achieved / peak,
-                    "traffic": (load_traffic("trail_ozaki") * sti.trail_flops / (4.0 * NB) / max(nblk, 1)
-                                if load_traffic("trail_ozaki") else None),
-                    "traffic_basis": "bytes per DM block (one launch of each of the four kernels): "
-                                     "21.8 B per C entry measured on the 4096^2 case "
-                                     "(profiles/oz_trailing_update_gauss4k.md) x the average m' n' "
-                                     "of this workload's blocks",
-                    "per_launch_basis": f"{prods} BF16 digit products x 4 m' n' k flops per DM "
-                                        f"block, {nblk} blocks",
-                    "fp64_equivalent_tflops": (sti.trail_flops / (sti.ms_trail / 1e3) / 1e12
-                                               if sti.ms_trail > 0 else 0.0)}
+            ncv = [int(x) for x in nc_i[:int(np.count_nonzero(nc_i))]]
+            entries, jb = 0.0, 0
+            for kb in ncv:
+                entries += float(m - jb) * float(max(0, n - jb - kb))
+                jb += kb
+            peak_t = peaks.get("bf16_tflops_sustained")
+            peak_b = peaks.get("hbm_gbs")
+            t_tensor = tflop / (peak_t * 1e12)
+            t_hbm = 24.0 * entries / (peak_b * 1e9)
+            sec = sti.ms_trail / 1e3
+            tr = load_traffic("trail_ozaki")
+            common = {"kernel": "Ozaki trailing update (k_oz_slice_v, k_oz_gemm1, k_oz_vtv + k_larft, "
+                                "k_oz_w2, k_oz_gemm2), FP16 tcgen05",
+                      "traffic": tr * entries / max(nblk, 1) if tr else None,
+                      "traffic_basis": "bytes per DM block (one launch of each kernel): 21.8 B per C "
+                                       "entry measured on the 4096^2 case "
+                                       "(profiles/oz_trailing_update_gauss4k.md) x the average C "
+                                       "entries of this workload's blocks",
+                      "fp64_equivalent_tflops": sti.trail_flops / sec / 1e12 if sec > 0 else 0.0,
+                      "tensor_frac": (tflop / sec / 1e12) / peak_t if sec > 0 else 0.0,
+                      "hbm_frac": (24.0 * entries / sec / 1e9) / peak_b if sec > 0 else 0.0}
+            if t_tensor >= t_hbm:
+                achieved = tflop / sec / 1e12 if sec > 0 else 0.0
+                roof = {"bound": "tensor", "achieved": achieved, "peak": peak_t,
+                        "peak_kind": f"{peak_kind} bf16 sustained (the phase runs inside a long step)",
+                        "unit": "TFLOP/s", "frac": achieved / peak_t,
+                        "per_launch_basis": f"{prods} FP16 digit products x 4 m' n' k flops per DM "
+                                            f"block, {nblk} blocks"}
+            else:
+                achieved = 24.0 * entries / sec / 1e9 if sec > 0 else 0.0
+                roof = {"bound": "hbm", "achieved": achieved, "peak": peak_b,
+                        "peak_kind": f"{peak_kind} HBM copy bandwidth", "unit": "GB/s",
+                        "frac": achieved / peak_b,
+                        "per_launch_basis": f"24 B per C entry (read by GEMM 1, read and written by "
+                                            f"GEMM 2) x m' (n' - k) per DM block, {nblk} blocks"}
+            roof.update(common)
         # accuracy of the instrumented factorisation, on the device:
         # ||A P - Q R||_F / ||A||_F with Q R formed by the library's DORMQR,
         # and the |R_kk| profile

@@ -156,25 +156,6 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_buf, int, long long* h
   }
 }
 
-// v 2^e rounded to nearest (ties to even), |v| < 2^62, built with integer
-// instructions (a 64-bit integer conversion runs on the FP64 pipe, the
-// scarce unit of the GEMM 2 epilogue); scales whose result would leave the
-// normal range take the conversion.
-__device__ __forceinline__ double oz_i64_scaled(long long v, int e) {
-  if (v == 0) return 0.0;
-  const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
-  unsigned long long m = (unsigned long long)(v < 0 ? -v : v);
-  const int lz = __clzll((long long)m);
-  const int ex = 1023 + 63 - lz + e;
-  if (ex <= 0 || ex >= 2046) return (double)v * pow2d(e);
-  m <<= lz;  // leading one at bit 63
-  const unsigned long long rest = m & 0x7FFull;
-  unsigned long long mant = m >> 11;  // 53 bits
-  mant += (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
-  // mant = 2^53 after rounding carries into the exponent field
-  return __longlong_as_double((long long)(sgn | (((unsigned long long)ex << 52) + mant - (1ull << 52))));
-}
-
 // GEMM 1 drain: the S levels of 8 accumulator columns (col0..col0+7) of
 // this thread's TMEM lane.  hi = sum_{L<=5} D_L 2^(8(5-L)) exactly in int64;
 // the low levels only need FP32 accuracy (they are accumulated in FP32
@@ -442,7 +423,8 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
 #pragma unroll
             for (int i = 0; i < OZ_G1_CPT; ++i) {
               const int a = OZ_G1_CPT * cgrp + i;
-              double v = fma((double)acc_hi[i], pow2d(e + 1 - 40), (double)acc_mid[i] * pow2d(e + 1 - 8 * (S + 1)));
+              // both terms built with integer instructions, one FP64 add
+              const double v = oz_i64_scaled(acc_hi[i], e + 1 - 40) + oz_f32_scaled(acc_mid[i], e + 1 - 8 * (S + 1));
               out[a] = a < k ? v : 0.0;
             }
           }

@@ -104,11 +104,52 @@ __device__ __forceinline__ double pow2d(int e) {
   return __longlong_as_double((long long)(e + 1023) << 52);
 }
 
+// |x| <= bound < 2^e  ->  returns e + 1, so |x| / 2^(e+1) < 1/2; 0 for a
+// bound that is not positive and finite.  Read off the exponent field with
+// integer instructions (frexp and FP64 compares would take the FP64 pipe).
 __device__ __forceinline__ int scale_exp_of(double bound) {
-  if (!(bound > 0.0) || !(bound < 1.7976931348623157e308)) return 0;
-  int e;
-  frexp(bound, &e);
-  return e + 1;  // |x| <= bound < 2^e  ->  |x| / 2^(e+1) < 1/2
+  const long long b = __double_as_longlong(bound);
+  if (b <= 0) return 0;  // negative, zero, or NaN with the sign bit set
+  const int E = (int)(b >> 52);
+  if (E == 0x7FF || b == 0x7FEFFFFFFFFFFFFFll) return 0;  // infinity, NaN, DBL_MAX (no 2^(e+1) above it)
+  if (E == 0) {              // subnormal
+    int e;
+    frexp(bound, &e);
+    return e + 1;
+  }
+  return E - 1021;  // bound in [2^(E-1023), 2^(E-1022))
+}
+
+// v 2^e rounded to nearest (ties to even), |v| < 2^62, built with integer
+// instructions (a 64-bit integer conversion runs on the FP64 pipe, the
+// scarce unit of the Ozaki epilogues); scales whose result would leave the
+// normal range take the conversion.
+__device__ __forceinline__ double oz_i64_scaled(long long v, int e) {
+  if (v == 0) return 0.0;
+  const unsigned long long sgn = (unsigned long long)v & 0x8000000000000000ull;
+  unsigned long long m = (unsigned long long)(v < 0 ? -v : v);
+  const int lz = __clzll((long long)m);
+  const int ex = 1023 + 63 - lz + e;
+  if (ex <= 0 || ex >= 2046) return (double)v * pow2d(e);
+  m <<= lz;  // leading one at bit 63
+  const unsigned long long rest = m & 0x7FFull;
+  unsigned long long mant = m >> 11;  // 53 bits
+  mant += (rest > 0x400ull || (rest == 0x400ull && (mant & 1ull))) ? 1ull : 0ull;
+  // mant = 2^53 after rounding carries into the exponent field
+  return __longlong_as_double((long long)(sgn | (((unsigned long long)ex << 52) + mant - (1ull << 52))));
+}
+
+// f 2^e exactly as a double, built from the FP32 bit pattern with integer
+// instructions; zero, subnormal or out-of-range inputs give 0 (the callers'
+// values there are far below the result's rounding).
+__device__ __forceinline__ double oz_f32_scaled(float f, int e) {
+  const unsigned u = __float_as_uint(f);
+  const int E8 = (int)((u >> 23) & 0xFF);
+  const int ex = E8 - 127 + 1023 + e;
+  if (E8 == 0 || E8 == 0xFF || ex <= 0 || ex >= 2047) return 0.0;
+  const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) | ((unsigned long long)ex << 52) |
+                                  ((unsigned long long)(u & 0x7FFFFFu) << 29);
+  return __longlong_as_double((long long)bits);
 }
 
 }  // namespace qrdm
