@@ -373,10 +373,10 @@ def run_ours(args):
             common = {"kernel": "Ozaki trailing update (k_oz_slice_v, k_oz_gemm1, k_oz_vtv + k_larft, "
                                 "k_oz_w2, k_oz_gemm2), FP16 tcgen05",
                       "traffic": tr * entries / max(nblk, 1) if tr else None,
-                      "traffic_basis": "bytes per DM block (one launch of each kernel): 21.8 B per C "
-                                       "entry measured on the 4096^2 case "
-                                       "(profiles/oz_trailing_update_gauss4k.md) x the average C "
-                                       "entries of this workload's blocks",
+                      "traffic_basis": "bytes per DM block (one launch of each kernel): 25.5 B per C "
+                                       "entry measured on the first 20 blocks of the 16384 x 8192 "
+                                       "workload (profiles/oz_trailing_update_lowrank16k.md) x the "
+                                       "average C entries of this workload's blocks",
                       "fp64_equivalent_tflops": sti.trail_flops / sec / 1e12 if sec > 0 else 0.0,
                       "tensor_frac": (tflop / sec / 1e12) / peak_t if sec > 0 else 0.0,
                       "hbm_frac": (24.0 * entries / sec / 1e9) / peak_b if sec > 0 else 0.0}
