@@ -482,21 +482,41 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
     // 4. apply H(i) to this CTA's rows, then the partials of column i+1
     if (!sm.tau_zero) {
       const int ncol_r = fjb - i - 1;
-      // flattened (column, row) index over all threads, advanced by a
-      // precomputed step instead of a division per entry
+      // flattened (column, row) index over all threads, two entries per
+      // iteration (both loaded before either is stored, so their shared
+      // memory round trips overlap), advanced by precomputed steps instead
+      // of a division per entry
       if (nr > 0) {
+        const int nt = (int)blockDim.x;
         int cc = tid / nr, rr = tid % nr;
-        const int dc = (int)blockDim.x / nr, dr = (int)blockDim.x % nr;
-        for (; cc < ncol_r; ) {
-          const int c = i + 1 + cc;
-          const int grow = grow0 + rr;
-          if (grow > i) S[(size_t)c * LS + rr] = fma(-x[rr], sm.tw[c], S[(size_t)c * LS + rr]);
-          else if (grow == i) S[(size_t)c * LS + rr] -= sm.tw[c];
+        int cc2 = (tid + nt) / nr, rr2 = (tid + nt) % nr;
+        const int dc = (2 * nt) / nr, dr = (2 * nt) % nr;
+        const int row_i = i - grow0;  // local row i (may be outside the slab)
+        const double* tw = sm.tw;
+        for (; cc < ncol_r;) {
+          const bool two = cc2 < ncol_r;
+          const int c1 = i + 1 + cc, c2 = i + 1 + (two ? cc2 : cc);
+          const int r2 = two ? rr2 : rr;
+          double* p1 = S + (size_t)c1 * LS + rr;
+          double* p2 = S + (size_t)c2 * LS + r2;
+          const double s1 = *p1, s2 = *p2, x1 = x[rr], x2 = x[r2], t1 = tw[c1], t2 = tw[c2];
+          if (rr > row_i) *p1 = fma(-x1, t1, s1);
+          else if (rr == row_i) *p1 = s1 - t1;
+          if (two) {
+            if (r2 > row_i) *p2 = fma(-x2, t2, s2);
+            else if (r2 == row_i) *p2 = s2 - t2;
+          }
           rr += dr;
           cc += dc;
           if (rr >= nr) {
             rr -= nr;
             ++cc;
+          }
+          rr2 += dr;
+          cc2 += dc;
+          if (rr2 >= nr) {
+            rr2 -= nr;
+            ++cc2;
           }
         }
       }
