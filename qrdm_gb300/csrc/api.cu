@@ -423,7 +423,8 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     {
       int msw = 2 * kmax + 2;
       size_t smem = sizeof(double) * 2 * msw + sizeof(int) * (2 * msw + 2 * kmax + 2 * msw) +
-                    sizeof(unsigned) * ((size_t)ceil_div(nloc, 32) + 4) + sizeof(double) * (size_t)kmax * kmax + 64;
+                    sizeof(unsigned) * ((size_t)ceil_div(nloc, 32) + 4) + sizeof(double) * (size_t)kmax * kmax +
+                    sizeof(unsigned long long) * 2 * (size_t)kmax + 64;
       if (smem + 1024 > c.smem_optin) return QRDM_ERR_UNSUPPORTED;
       k_dm_pick<<<1, 256, smem, s>>>(c.cand.as<Cand>(), c.gram.as<double>(), km, nloc, kmax, P.delta,
                                      P.jpvt + j, nrm + j, c.perm.as<int2>(), d_st);

@@ -409,6 +409,7 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // layout: [stage doubles 2*maxsw][stage ints 2*maxsw][sel kmax][pos kmax]
   //         [swapA maxsw][swapB maxsw][bitmap ceil(ncols/32) words]
+  //         [cosines nc x nc][conflict masks nc x 2 words of 64 bits]
   int maxsw = 2 * kmax + 2;
   double* s_nv = reinterpret_cast<double*>(smem_raw);
   int* s_jv = reinterpret_cast<int*>(s_nv + 2 * maxsw);
@@ -436,35 +437,46 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
     }
   }
   __syncthreads();
-  // greedy in norm order (warp 0): candidate i is taken iff every |cos| with
-  // the columns taken so far is < delta; the max over taken columns is a
-  // warp reduction
-  if (threadIdx.x < 32) {
-    const int lane = threadIdx.x;
-    int nsel = 1;
-    if (lane == 0) {
+  // greedy in norm order: candidate i is taken iff every |cos| with the
+  // columns taken so far is < delta (and fewer than kmax are taken).  All
+  // warps first turn the comparisons into conflict masks (bit j of mask i:
+  // j < i and NOT |cos(j, i)| < delta, compared as bit patterns on the
+  // integer pipes); then one thread runs the scan with 128-bit ANDs.
+  {
+    unsigned long long* s_mask = reinterpret_cast<unsigned long long*>(s_g + (size_t)nc * nc);  // [nc][2]
+    const unsigned long long delta_bits = abs_bits(delta);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)blockDim.x >> 5;
+    for (int i = wid; i < nc; i += nw) {
+      unsigned words[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = 32 * q + lane;
+        const bool conflict = j < i && !(abs_bits(s_g[(size_t)j * nc + i]) < delta_bits);
+        words[q] = __ballot_sync(0xffffffffu, conflict);
+      }
+      if (lane == 0) {
+        s_mask[2 * i] = (unsigned long long)words[0] | ((unsigned long long)words[1] << 32);
+        s_mask[2 * i + 1] = (unsigned long long)words[2] | ((unsigned long long)words[3] << 32);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      unsigned long long sel0 = 1ull, sel1 = 0ull;
+      int nsel = 1;
       s_sel[0] = cand[0].idx;
       s_pos[0] = 0;
-    }
-    __syncwarp();
-    const unsigned long long delta_bits = abs_bits(delta);
-    for (int i = 1; i < nc; ++i) {
-      unsigned long long worst = 0ull;  // max |cos| as bits (integer pipes)
-      for (int q = lane; q < nsel; q += 32) {
-        const unsigned long long b = abs_bits(s_g[s_pos[q] * nc + i]);
-        worst = b > worst ? b : worst;
-      }
-      worst = warp_max_u64(worst);
-      if (worst < delta_bits && nsel < kmax) {
-        if (lane == 0) {
+      for (int i = 1; i < nc; ++i) {
+        const unsigned long long m0 = s_mask[2 * i], m1 = s_mask[2 * i + 1];
+        if (nsel < kmax && (m0 & sel0) == 0ull && (m1 & sel1) == 0ull) {
+          if (i < 64) sel0 |= 1ull << i;
+          else sel1 |= 1ull << (i - 64);
           s_pos[nsel] = i;
           s_sel[nsel] = cand[i].idx;
+          ++nsel;
         }
-        ++nsel;
       }
-      __syncwarp();
+      s_nsel = nsel;
     }
-    if (lane == 0) s_nsel = nsel;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -486,12 +498,16 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   } while (0)
     int nswap = 0;
     int jb = 0, jt = ncols - 1;
+    // once the last column is unmarked it stays so (later exchanges move
+    // marks from a marked jc down to jb < jc <= jt), so its test is cached
+    bool jt_marked = true;
     for (int s = 0; s < nsel; ++s) {
       int jc = s_sel[s];
-      while (jb < jt && MARK(jt) == 1u) {
+      while (jt_marked && jb < jt && MARK(jt) == 1u) {
         XCHG(jt, jb);
         while (jb < ncols && MARK(jb) == 1u) ++jb;
       }
+      jt_marked = jt_marked && jb < jt && MARK(jt) == 1u;
       if (MARK(jc) != 1u) continue;
       while (jb < ncols && MARK(jb) == 1u) ++jb;
       if (jc <= jb || jc < nsel) continue;
@@ -522,14 +538,18 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
       int s = e >> 1;
       dst = (e & 1) ? s_swb[s] : s_swa[s];
       keep = 1;
-      for (int t = 0; t < s && keep; ++t)
+      // (loop bodies unrolled: the swap-list loads do not depend on the
+      // running state, so they are issued ahead of the compares)
+#pragma unroll 8
+      for (int t = 0; t < s; ++t)
         if (s_swa[t] == dst || s_swb[t] == dst) keep = 0;
       if (keep && (e & 1) && s_swa[s] == dst) keep = 0;
       if (keep) {
         int x = dst;
+#pragma unroll 8
         for (int t = nswap - 1; t >= 0; --t) {
-          if (x == s_swa[t]) x = s_swb[t];
-          else if (x == s_swb[t]) x = s_swa[t];
+          const int a = s_swa[t], b = s_swb[t];
+          x = x == a ? b : (x == b ? a : x);
         }
         src = x;
         if (src == dst) keep = 0;
