@@ -607,10 +607,23 @@ __global__ void __launch_bounds__(256) k_permute_columns(double* __restrict__ A,
   if (np <= 0) return;
   if (np > max_entries) np = max_entries;
   int r0 = blockIdx.x * ROWS;
-  for (int e = threadIdx.x; e < np * ROWS; e += blockDim.x) {
-    int t = e / ROWS, rr = e % ROWS;
-    int r = r0 + rr;
-    if (r < m) s[t * ROWS + rr] = A[(size_t)(j + perm[t].y) * lda + r];
+  // eight independent loads in flight per thread before their shared stores
+  // (one load at a time would expose a full memory latency per entry)
+  constexpr int U = 8;
+  const int total = np * ROWS, step = (int)blockDim.x;
+  for (int base = threadIdx.x; base < total; base += U * step) {
+    double v[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = base + u * step;
+      const int t = e / ROWS, r = r0 + e % ROWS;
+      v[u] = (e < total && r < m) ? __ldcs(A + (size_t)(j + perm[t].y) * lda + r) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int e = base + u * step;
+      if (e < total) s[e] = v[u];
+    }
   }
   __syncthreads();
   for (int e = threadIdx.x; e < np * ROWS; e += blockDim.x) {
