@@ -70,6 +70,7 @@ int set_kernel_attributes(int big) {
     CK(cudaFuncSetAttribute(k_trail_w_reduce, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_qp3_gemv, cudaFuncAttributeMaxDynamicSharedMemorySize, 65536));
     if (oz_set_attributes()) return QRDM_ERR_CUDA;
+    if (topk_set_attributes()) return QRDM_ERR_CUDA;
     if (batched_set_attributes()) return QRDM_ERR_CUDA;
   }
   return 0;

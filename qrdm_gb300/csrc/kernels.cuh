@@ -64,6 +64,8 @@ __global__ void k_norm_recompute(const double* A, long long lda, int j, int m, c
 __global__ void k_topk_tile(const double* nrm, const Cand* in_cand, int count, int kmax,
                             Cand* out);
 constexpr int kTopkRadixMax = 65536;  // largest count the radix top-k takes
+constexpr int kTopkKeysMax = 16384;   // largest count whose keys it stages in shared memory
+int topk_set_attributes();             // dynamic shared memory of the radix top-k (per device)
 void launch_topk_radix(int count, cudaStream_t s, const double* nrm, int kmax, double tau_rel, Cand* cand,
                        BlockState* st);
 void launch_topk_final(int count, cudaStream_t st_, const Cand* in_cand, const double* nrm, int kmax,

@@ -46,26 +46,34 @@ __global__ void k_norm_downdate(const double* __restrict__ A, long long lda, int
   int fjb_cmp = st->fjb_cmp;
   int c0 = j + fjb_cmp;
   int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= n) return;
-  double w = nrm[c];
-  if (w == 0.0) return;
-  const double* col = A + (size_t)c * lda + j;
-  double s = 0.0;
-  for (int i = 0; i < fjb_cmp; ++i) s = mul_add_rn(col[i], col[i], s);
-  double t = sqrt(fabs(s)) / w;
-  double d2 = (t + 1.0) * (1.0 - t);
-  t = (0.0 >= d2) ? 0.0 : d2;
-  double r = w / nrm_exact[c];
-  double t2 = t * (r * r);
-  const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53)
-  if (t2 <= tol3z) {
-    int slot = atomicAdd(&st->recompute, 1);
-    list[slot] = c;
-  } else {
-    w *= sqrt(t);
-    nrm[c] = w;
-    atomic_max_nonneg(&st->maxnrm_bits, w);
+  // the new maximum is reduced over the warp first: one atomic per warp
+  // instead of one per column on the same address
+  unsigned long long mx = 0ull;
+  if (c < n) {
+    double w = nrm[c];
+    if (w != 0.0) {
+      const double* col = A + (size_t)c * lda + j;
+      double s = 0.0;
+#pragma unroll 8
+      for (int i = 0; i < fjb_cmp; ++i) s = mul_add_rn(col[i], col[i], s);
+      double t = sqrt(fabs(s)) / w;
+      double d2 = (t + 1.0) * (1.0 - t);
+      t = (0.0 >= d2) ? 0.0 : d2;
+      double r = w / nrm_exact[c];
+      double t2 = t * (r * r);
+      const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53)
+      if (t2 <= tol3z) {
+        int slot = atomicAdd(&st->recompute, 1);
+        list[slot] = c;
+      } else {
+        w *= sqrt(t);
+        nrm[c] = w;
+        if (w > 0.0) mx = (unsigned long long)__double_as_longlong(w);
+      }
+    }
   }
+  mx = warp_max_u64(mx);
+  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&st->maxnrm_bits, mx);
 }
 
 // From-scratch partial norms of the listed columns over the rows below the

@@ -82,13 +82,23 @@ constexpr int kTopkList = 512;
 
 __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ nrm, int count, int kmax,
                                                      double tau_rel, Cand* __restrict__ cand,
-                                                     BlockState* __restrict__ st) {
+                                                     BlockState* __restrict__ st, int cached) {
+  // cached: the keys are read from global memory once into shared memory
+  // (count <= kTopkKeysMax), and every pass reads them there
+  extern __shared__ unsigned long long s_keys[];
   __shared__ unsigned hist[256];
   __shared__ Cand list[kTopkList];
   __shared__ int s_nlist, s_above, s_d;
   __shared__ int s_scan[32];
   const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
   const int want = min(kmax, count);
+  if (cached) {
+    for (int i = tid; i < count; i += blockDim.x) s_keys[i] = (unsigned long long)__double_as_longlong(nrm[i]);
+    __syncthreads();
+  }
+  auto key_at = [&](int i) -> unsigned long long {
+    return cached ? s_keys[i] : (unsigned long long)__double_as_longlong(nrm[i]);
+  };
   unsigned long long prefix = 0ull, mask = 0ull;
   int need = want;  // entries still to take from the current bucket
   int above = 0;    // entries strictly above the current bucket
@@ -97,7 +107,7 @@ __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ 
     for (int b = tid; b < 256; b += blockDim.x) hist[b] = 0u;
     __syncthreads();
     for (int i = tid; i < count; i += blockDim.x) {
-      const unsigned long long key = (unsigned long long)__double_as_longlong(nrm[i]);
+      const unsigned long long key = key_at(i);
       if ((key & mask) == prefix) atomicAdd(&hist[(key >> shift) & 255u], 1u);
     }
     __syncthreads();
@@ -145,8 +155,8 @@ __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ 
   if (small) {
     // every entry at or above the bucket fits the list
     for (int i = tid; i < count; i += blockDim.x) {
-      const double v = nrm[i];
-      const unsigned long long key = (unsigned long long)__double_as_longlong(v);
+      const unsigned long long key = key_at(i);
+      const double v = __longlong_as_double((long long)key);
       if ((key & mask) >= prefix) {
         const int slot = atomicAdd(&s_nlist, 1);
         if (slot < kTopkList) list[slot] = Cand{v, i, 0};
@@ -160,8 +170,8 @@ __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ 
     const int i0 = tid * chunk, i1 = min(count, i0 + chunk);
     int ties = 0;
     for (int i = i0; i < i1; ++i) {
-      const double v = nrm[i];
-      const unsigned long long key = (unsigned long long)__double_as_longlong(v);
+      const unsigned long long key = key_at(i);
+      const double v = __longlong_as_double((long long)key);
       if (key > prefix) {
         const int slot = atomicAdd(&s_nlist, 1);
         if (slot < kTopkList) list[slot] = Cand{v, i, 0};
@@ -191,8 +201,8 @@ __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ 
     __syncthreads();
     int rank = s_scan[w] + incl - ties;
     for (int i = i0; i < i1 && rank < need; ++i) {
-      const double v = nrm[i];
-      const unsigned long long key = (unsigned long long)__double_as_longlong(v);
+      const unsigned long long key = key_at(i);
+      const double v = __longlong_as_double((long long)key);
       if (key == prefix) {
         const int slot = atomicAdd(&s_nlist, 1);
         if (slot < kTopkList) list[slot] = Cand{v, i, 0};
@@ -216,9 +226,16 @@ __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ 
   }
 }
 
+int topk_set_attributes() {
+  return cudaFuncSetAttribute(k_topk_radix, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)(sizeof(unsigned long long) * kTopkKeysMax)) == cudaSuccess ? 0 : 1;
+}
+
 void launch_topk_radix(int count, cudaStream_t s, const double* nrm, int kmax, double tau_rel, Cand* cand,
                        BlockState* st) {
-  k_topk_radix<<<1, 1024, 0, s>>>(nrm, count, kmax, tau_rel, cand, st);
+  const int cached = count <= kTopkKeysMax ? 1 : 0;
+  const size_t smem = cached ? sizeof(unsigned long long) * (size_t)count : 0;
+  k_topk_radix<<<1, 1024, smem, s>>>(nrm, count, kmax, tau_rel, cand, st, cached);
 }
 
 constexpr int TOPK_TILE = kTopkTile;
