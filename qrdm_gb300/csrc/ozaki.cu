@@ -132,6 +132,40 @@ __device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32
 // FP32 -> int32 conversion.
 __device__ __forceinline__ int f32_small_int(float x) { return __float_as_int(x + 12582912.0f) - 0x4B400000; }
 
+// s = 7: the GEMM 2 levels of 8 columns combined directly into comb (see the
+// epilogue).  With K <= 64, |D_L| <= c_L 2^20 (c_L = L - 1 digit pairs), so
+// adjacent levels pair up exactly in 32-bit integers, P1 = D2 256 + D3,
+// P2 = D4 256 + D5, P3 = D6 256 + D7 (|P3| < 5.1 2^28), and
+// comb = hi 2^17 + (mid >> 7) = P1 2^33 + P2 2^17 + P3 2 + (D8 >> 7): three
+// 64-bit shifts and adds per entry instead of one per level.
+__device__ __forceinline__ void oz_comb8_s7(uint32_t taddr_buf, uint32_t col, long long* comb) {
+  int p1[8], p2[8], p3[8], d8[8];
+#pragma unroll
+  for (int L = 2; L <= 8; ++L) {
+    uint32_t r[8];
+    asm volatile("tcgen05.ld.sync.aligned.32x32b.x8.b32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+                   "=r"(r[7])
+                 : "r"(taddr_buf + (uint32_t)((L - 2) * 32) + col)
+                 : "memory");
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+      const float x = __uint_as_float(r[i]);
+      if (L == 2) p1[i] = f32_small_int(x) * 256;
+      else if (L == 3) p1[i] += f32_small_int(x);
+      else if (L == 4) p2[i] = f32_small_int(x) * 256;
+      else if (L == 5) p2[i] += f32_small_int(x);
+      else if (L == 6) p3[i] = f32_to_int(x) * 256;
+      else if (L == 7) p3[i] += f32_to_int(x);
+      else d8[i] = f32_to_int(x);
+    }
+  }
+#pragma unroll
+  for (int i = 0; i < 8; ++i)
+    comb[i] = ((long long)p1[i] << 33) + ((long long)p2[i] << 17) + ((long long)p3[i] << 1) + (long long)(d8[i] >> 7);
+}
+
 template <int S>
 __device__ __forceinline__ void oz_levels8(uint32_t taddr_buf, int, long long* hi, long long* mid, uint32_t col) {
 #pragma unroll
@@ -687,8 +721,12 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
       tc::fence_after_sync();
 #pragma unroll
       for (int jb = 0; jb < OZ_G2_CPW; jb += 8) {
-        long long hi[8], mid[8];
-        oz_levels8<S>(tl + (uint32_t)(b * 256), 0, hi, mid, (uint32_t)(OZ_G2_CPW * ch + jb));
+        long long hi[8], mid[8], comb8[8];
+        if constexpr (S == 7) {
+          oz_comb8_s7(tl + (uint32_t)(b * 256), (uint32_t)(OZ_G2_CPW * ch + jb), comb8);
+        } else {
+          oz_levels8<S>(tl + (uint32_t)(b * 256), 0, hi, mid, (uint32_t)(OZ_G2_CPW * ch + jb));
+        }
         if (jb + 8 >= OZ_G2_CPW) {
           tc::fence_before_sync();
           __syncwarp();
@@ -705,7 +743,9 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
               // instructions) and subtracted with the one FP64 operation
               const int e = 1 + g.wexp[cw];  // V scale 2^1 times W2 column scale
               constexpr int msh = 8 * (S + 1) - 40 - 17;
-              const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
+              long long comb;
+              if constexpr (S == 7) comb = comb8[j];
+              else comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
               const double res = cv[jb + j] - oz_i64_scaled(comb, e - 57);
               g.W0[(size_t)c * g.lda + r] = res;
             }
