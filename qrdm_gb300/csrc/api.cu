@@ -404,7 +404,9 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
         k_gram_bf16<<<nchunk, 128, 0, s>>>(P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
                                            c.gram_part.as<double>());
         RET(check_launch());
-        k_gram_reduce<<<ceil_div(km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
+        k_gram_reduce_bf16<<<ceil_div(8 * km * km, 256), 256, 0, s>>>(
+            reinterpret_cast<const float*>(c.gram_part.as<double>()), nchunk, km, c.cand.as<Cand>(), d_st,
+            c.gram.as<double>());
         RET(check_launch());
         const int npair = kmax * (kmax - 1) / 2;
         k_gram_recheck<<<std::max(1, ceil_div(npair * 32, 256)), 256, 0, s>>>(
@@ -416,7 +418,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
         launch_gram_partial(km, nchunk, s, P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
                             c.gram_part.as<double>());
         RET(check_launch());
-        k_gram_reduce<<<ceil_div(km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
+        k_gram_reduce<<<ceil_div(8 * km * km, 256), 256, 0, s>>>(c.gram_part.as<double>(), nchunk, km, d_st, c.gram.as<double>());
         RET(check_launch());
       }
     }

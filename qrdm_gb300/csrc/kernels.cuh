@@ -77,6 +77,8 @@ __global__ void k_gram_reduce(const double* part, int nchunk, int km, const Bloc
                               double* gram);
 __global__ void k_gram_bf16(const double* A, long long lda, int j, int mloc, int rows_per_chunk,
                             const Cand* cand, BlockState* st, double* part);
+__global__ void k_gram_reduce_bf16(const float* part, int nchunk, int km, const Cand* cand,
+                                   const BlockState* st, double* gram);
 __global__ void k_gram_recheck(const double* A, long long lda, int j, int mloc, const Cand* cand,
                                double delta, double margin, int km, BlockState* st, double* gram);
 __global__ void k_dm_pick(const Cand* cand, const double* gram, int km, int ncols, int kmax,

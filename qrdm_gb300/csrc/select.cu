@@ -21,6 +21,7 @@
 
 #include "common.cuh"
 #include "kernels.cuh"
+#include "ozaki_digits.cuh"
 #include "tc.cuh"
 
 namespace qrdm {
@@ -392,26 +393,71 @@ __global__ void __launch_bounds__(256) k_gram_partial(const double* __restrict__
     for (int b = 0; b < SUB; ++b) out[(tp + 16 * a) * KM + (tq + 16 * b)] = acc[a][b];
 }
 
-// gram[p][q] = sum over chunks (fixed order) of part[chunk][p][q].
+// gram[p][q] = sum over chunks of part[chunk][p][q], in a fixed order:
+// eight threads per entry each sum every eighth chunk (eight loads in
+// flight ahead of the additions), then a fixed shuffle tree (one thread per
+// entry left one long chain of dependent loads per entry).
 __global__ void k_gram_reduce(const double* __restrict__ part, int nchunk, int km,
                               const BlockState* __restrict__ st, double* __restrict__ gram) {
   int nc = st->nc;
   if (nc <= 1) return;
-  int e = blockIdx.x * blockDim.x + threadIdx.x;
-  if (e >= km * km) return;
-  // fixed order; eight loads in flight ahead of the additions
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = gt >> 3, q = gt & 7;
   const size_t stride = (size_t)km * km;
   double s = 0.0;
-  int c = 0;
-  for (; c + 8 <= nchunk; c += 8) {
-    double v[8];
+  if (e < km * km) {
+    int c = q;
+    for (; c + 56 < nchunk; c += 64) {
+      double v[8];
 #pragma unroll
-    for (int u = 0; u < 8; ++u) v[u] = __ldcg(part + (size_t)(c + u) * stride + e);
+      for (int u = 0; u < 8; ++u) v[u] = __ldcg(part + (size_t)(c + 8 * u) * stride + e);
 #pragma unroll
-    for (int u = 0; u < 8; ++u) s += v[u];
+      for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (; c < nchunk; c += 8) s += __ldcg(part + (size_t)c * stride + e);
   }
-  for (; c < nchunk; ++c) s += __ldcg(part + (size_t)c * stride + e);
-  gram[e] = s;
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  s += __shfl_xor_sync(0xffffffffu, s, 4);
+  if (e < km * km && q == 0) gram[e] = s;
+}
+
+// The BF16 Gram's FP32 partials (k_gram_bf16): gram[p][q] = (sum over
+// chunks, fixed order as in k_gram_reduce, in FP32) * (2^e_p / norm_p) *
+// (2^e_q / norm_q).  FP32 sums are ample for a pre-filter whose decisions
+// near delta are all rechecked in FP64.
+__global__ void k_gram_reduce_bf16(const float* __restrict__ part, int nchunk, int km,
+                                   const Cand* __restrict__ cand, const BlockState* __restrict__ st,
+                                   double* __restrict__ gram) {
+  int nc = st->nc;
+  if (nc <= 1) return;
+  const int gt = blockIdx.x * blockDim.x + threadIdx.x;
+  const int e = gt >> 3, q = gt & 7;
+  const size_t stride = (size_t)km * km;
+  float s = 0.f;
+  if (e < km * km) {
+    int c = q;
+    for (; c + 56 < nchunk; c += 64) {
+      float v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) v[u] = __ldcg(part + (size_t)(c + 8 * u) * stride + e);
+#pragma unroll
+      for (int u = 0; u < 8; ++u) s += v[u];
+    }
+    for (; c < nchunk; c += 8) s += __ldcg(part + (size_t)c * stride + e);
+  }
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  s += __shfl_xor_sync(0xffffffffu, s, 2);
+  s += __shfl_xor_sync(0xffffffffu, s, 4);
+  if (e < km * km && q == 0) {
+    const int a = e / km, b = e % km;
+    double f = 0.0;
+    if (a < nc && b < nc) {
+      const double na = cand[a].val, nb = cand[b].val;
+      f = (pow2d(scale_exp_of(na)) / na) * (pow2d(scale_exp_of(nb)) / nb);
+    }
+    gram[e] = (double)s * f;
+  }
 }
 
 // Greedy pick + permute_marked replay.  One CTA; thread 0 runs the
@@ -667,16 +713,38 @@ void launch_gram_partial(int km, int nchunk, cudaStream_t s, const double* A, lo
 // cosine is within 2^-8 of the exact one; the default margin is 2^-7.
 // One CTA per row chunk: the candidates fill rows p < nc of one 128 x 64
 // K-major tile per 64-row block (rows >= nc zero); the same tile's first 64
-// rows serve as the N operand, D = 128 x 64 in TMEM (FP32), of which the
-// first nc x nc block is written out (as FP64 partials, summed by
-// k_gram_reduce in a fixed order).
+// rows serve as the N operand, D = 128 x 64 in TMEM (FP32), which is written
+// out as FP32 partials and summed by k_gram_reduce_bf16 in a fixed order.
+// No FP64 instruction: each column is scaled by a power of two 2^-e_p
+// (e_p from its partial norm, so |x| 2^-e_p <= 1/2) and rounded to BF16
+// with integer instructions (bf16_scaled); the reduction applies
+// 2^e_p / norm_p per row and column once per entry.
+
+// x 2^-e rounded to BF16 (nearest, ties to even) with integer instructions;
+// results below BF16's normal range are flushed to zero (their cosine
+// contribution is far below the recheck margin).
+__device__ __forceinline__ uint32_t bf16_scaled(double x, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+  const uint32_t hi = (uint32_t)(b >> 32), lo = (uint32_t)b;
+  const uint32_t sgn = (hi >> 16) & 0x8000u;
+  const int E = (int)((hi >> 20) & 0x7FF);
+  const int E8 = E - 1023 + 127 - e;
+  if (E == 0 || E8 <= 0) return sgn;
+  if (E8 >= 255) return sgn | 0x7F80u;
+  const uint32_t m7 = (hi >> 13) & 0x7Fu;
+  const uint32_t half = (hi >> 12) & 1u;
+  const uint32_t sticky = ((hi & 0xFFFu) | lo) != 0u ? 1u : 0u;
+  uint32_t r = ((uint32_t)E8 << 7) | m7;
+  r += half & (sticky | (m7 & 1u));  // carries into the exponent as needed
+  return sgn | r;
+}
 
 __global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A, long long lda, int j,
                                                    int mloc, int rows_per_chunk,
                                                    const Cand* __restrict__ cand,
                                                    BlockState* __restrict__ st, double* __restrict__ part) {
   __shared__ __align__(1024) unsigned char tile[128 * 128];
-  __shared__ double s_rc[64];
+  __shared__ int s_e[64];
   __shared__ int s_col[64];
   __shared__ uint64_t bar;
   __shared__ uint32_t s_tmem;
@@ -686,7 +754,7 @@ __global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A,
   const int r_begin = blockIdx.x * rows_per_chunk;
   const int r_end = min(mloc, r_begin + rows_per_chunk);
   if (tid < 64) {
-    s_rc[tid] = tid < nc ? 1.0 / cand[tid].val : 0.0;
+    s_e[tid] = tid < nc ? scale_exp_of(cand[tid].val) : 0;
     s_col[tid] = tid < nc ? j + cand[tid].idx : 0;
   }
   // rows >= 64 of the tile stay zero for the whole kernel
@@ -707,14 +775,13 @@ __global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A,
     for (int e = tid; e < 64 * 32; e += blockDim.x) {
       const int p = e >> 5, kp = e & 31;
       const int r = r0 + 2 * kp;
-      float v0 = 0.f, v1 = 0.f;
+      uint32_t v0 = 0u, v1 = 0u;
       if (p < nc) {
         const double* col = A + (size_t)s_col[p] * lda + j;
-        if (r < r_end) v0 = (float)(s_rc[p] * col[r]);
-        if (r + 1 < r_end) v1 = (float)(s_rc[p] * col[r + 1]);
+        if (r < r_end) v0 = bf16_scaled(col[r], s_e[p]);
+        if (r + 1 < r_end) v1 = bf16_scaled(col[r + 1], s_e[p]);
       }
-      __nv_bfloat162 b2 = __floats2bfloat162_rn(v0, v1);
-      *reinterpret_cast<__nv_bfloat162*>(tile + tc::sw128_offset(p, 2 * kp)) = b2;
+      *reinterpret_cast<uint32_t*>(tile + tc::sw128_offset(p, 2 * kp)) = v0 | (v1 << 16);
     }
     tc::fence_async_smem();
     __syncthreads();
@@ -744,11 +811,13 @@ __global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A,
       float v[16];
       tc::tmem_ld16(tmem + ((uint32_t)(32 * w) << 16) + c0, v);
       tc::tmem_wait_ld();
-      for (int i = 0; i < 16; ++i) part[(size_t)blockIdx.x * 64 * 64 + p * 64 + c0 + i] = (double)v[i];
+      float* pf = reinterpret_cast<float*>(part) + (size_t)blockIdx.x * 64 * 64 + p * 64 + c0;
+      for (int i = 0; i < 16; ++i) pf[i] = v[i];
     }
   } else if (w < 2 && first) {  // empty chunk: zero partial
     const int p = 32 * w + lane;
-    for (int q = 0; q < 64; ++q) part[(size_t)blockIdx.x * 64 * 64 + p * 64 + q] = 0.0;
+    float* pf = reinterpret_cast<float*>(part) + (size_t)blockIdx.x * 64 * 64 + p * 64;
+    for (int q = 0; q < 64; ++q) pf[q] = 0.f;
   }
   tc::fence_before_sync();
   __syncthreads();
