@@ -408,7 +408,8 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
         }
         if (spins > 32) __nanosleep(20);
       }
-      __threadfence();
+      // (the acquire load orders this CTA's reads of the totals after the
+      // arrivals; the block barrier passes that on to the other threads)
     }
     __syncthreads();
     PPH(2);
