@@ -396,7 +396,8 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
     __syncthreads();
     PPH(0);
     if (tid == 0) {
-      __threadfence();
+      // release: this thread's and (through the block barrier) every other
+      // thread's additions and stores are ordered before the arrival
       red_release_add_u32(p.bar, 1u);
       const unsigned target = (unsigned)G * (unsigned)(i + 1);
       unsigned spins = 0;
