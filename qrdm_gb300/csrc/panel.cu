@@ -423,33 +423,34 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
       const unsigned long long* tot = acc + panel_acc_offset(i, fjb);
       for (int c = i + tid; c < fjb; c += blockDim.x) s_row[c] = __ldcg(rowb + c);
       for (int sl = tid; sl < nslot; sl += blockDim.x) sm.red[sl] = limbs_value(tot + (size_t)kLimbs * sl);
+      // 3a. thread 0 has just formed alpha = A(i,i) and the squared norm
+      //     below it: beta (and the exit test) before the block barrier.
+      //     FP64 instructions with one active lane still take the SM
+      //     sub-partition's FP64 pipe for a whole warp's time, so the
+      //     scalar chain is kept short and split across warps on different
+      //     sub-partitions (3b); the exit test compares squares.
+      if (tid == 0) {
+        const double alpha = s_row[i], red0 = sm.red[0];
+        sm.tau_zero = 1;
+        sm.beta = alpha;
+        if (p.mloc - i > 1) {
+          const double t = sm.thres * sm.sc[i];  // thres in this column's scaled units
+          if (i > 0 && p.allow_exit && red0 < t * t) {
+            sm.exit_flag = 1;
+          } else if (red0 != 0.0) {
+            sm.beta = -sign_of(sqrt(fma(alpha, alpha, red0)), alpha);
+            sm.tau_zero = 0;
+          }
+        }
+        if (!sm.exit_flag && i == 0 && fjb > 1 && p.tau_rel > 0.0)
+          sm.thres = p.tau_rel * fabs(sm.beta) * sm.sc_inv[0];
+      }
     }
     __syncthreads();
     PPH(3);
-    // 3. dlarfg scalars.  FP64 instructions with one active lane still take
-    //    the SM sub-partition's FP64 pipe for a whole warp's time, so the
-    //    chain is kept short and split across warps on different
-    //    sub-partitions: beta first (thread 0; the exit test compares
-    //    squares, no square root), then 1/beta and tau (warp 0) beside
-    //    1/(alpha - beta) (warp 1), then tau w_c = tau C(i,c) - (x.C_c)/beta
-    //    (tau / (alpha - beta) = -1/beta) beside the scaling of x.
-    if (tid == 0) {
-      const double alpha = s_row[i], red0 = sm.red[0];
-      sm.tau_zero = 1;
-      sm.beta = alpha;
-      if (p.mloc - i > 1) {
-        const double t = sm.thres * sm.sc[i];  // thres in this column's scaled units
-        if (i > 0 && p.allow_exit && red0 < t * t) {
-          sm.exit_flag = 1;
-        } else if (red0 != 0.0) {
-          sm.beta = -sign_of(sqrt(fma(alpha, alpha, red0)), alpha);
-          sm.tau_zero = 0;
-        }
-      }
-      if (!sm.exit_flag && i == 0 && fjb > 1 && p.tau_rel > 0.0)
-        sm.thres = p.tau_rel * fabs(sm.beta) * sm.sc_inv[0];
-    }
-    __syncthreads();
+    // 3b. then 1/beta and tau (warp 0) beside 1/(alpha - beta) (warp 1), then
+    //     tau w_c = tau C(i,c) - (x.C_c)/beta (tau / (alpha - beta) = -1/beta)
+    //     beside the scaling of x.
     if (sm.exit_flag == 1) {
       done = i;
       break;
