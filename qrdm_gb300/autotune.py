@@ -4,7 +4,7 @@ The batched kernel has two free choices per batch: the DM block size nb
 (which also selects the kernel's shared-memory layout: nb <= 32 uses the
 compact layout that leaves room for the tensor-core tiles) and the
 arithmetic of the trailing update, Gram and V^T V (``"fp64"`` or
-``"mixed"``, the Ozaki split on the BF16 tensor cores).  The tuner times
+``"mixed"``, the Ozaki split on the tensor cores).  The tuner times
 each candidate on the batch itself (or a seeded sample of it: the largest
 problems plus a uniform draw, which keeps the makespan structure) with CUDA
 events and keeps the fastest.  Results are cached per batch signature

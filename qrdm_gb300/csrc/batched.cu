@@ -312,7 +312,7 @@ __device__ __forceinline__ void oz_mma_block(uint32_t d, uint32_t a, uint32_t b,
   for (int p = 1; p <= OZS; ++p) {
     const uint32_t idesc = tc::idesc_f16_f32(128, 32 * (OZS + 1 - p));
     for (int kk = 0; kk < nkk; ++kk)
-      tc::mma_bf16(d + (uint32_t)((p - 1) * 32), tc::desc_sw128(a + (uint32_t)(p - 1) * 16384u + kk * 32),
+      tc::mma_f16(d + (uint32_t)((p - 1) * 32), tc::desc_sw128(a + (uint32_t)(p - 1) * 16384u + kk * 32),
                    tc::desc_sw128(b + kk * 32), idesc, (first && p == 1 && kk == 0) ? 0u : 1u);
   }
 }
@@ -345,7 +345,7 @@ __device__ void cta_gram_tc(OzCtx& z, int mloc, int nc, F f, double* g, int gs, 
     if (tid == 0) {
       tc::fence_after_sync();
       for (int kk = 0; kk < 4; ++kk)
-        tc::mma_bf16(z.tmem, tc::desc_sw128(asm_ + kk * 32), tc::desc_sw128(bsm + kk * 32), idesc,
+        tc::mma_f16(z.tmem, tc::desc_sw128(asm_ + kk * 32), tc::desc_sw128(bsm + kk * 32), idesc,
                      (r0 > 0 || kk > 0) ? 1u : 0u);
       tc::mma_commit(z.bar);
     }

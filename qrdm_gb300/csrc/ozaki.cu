@@ -26,7 +26,6 @@
 // uses the fixed scale 2^1.  The columns of C use 2^(E+1) with E the binary
 // exponent of their partial norm (an upper bound of every entry).  The
 // columns of W2 use 2^(E+1) of their own max.
-#include <cuda_bf16.h>
 
 #include "common.cuh"
 #include "kernels.cuh"
@@ -116,7 +115,7 @@ __device__ __forceinline__ void oz_issue(uint32_t tmem, uint32_t a_tiles, uint32
       for (int kk = kk0; kk < kk1; ++kk) {
         uint64_t ad = tc::desc_sw128(a_tiles + (uint32_t)(p - 1) * a_stride + kk * 32);
         uint64_t bd = tc::desc_sw128(b_tiles + (uint32_t)(q0 - 1) * 8192u + kk * 32);
-        tc::mma_bf16(tmem + dcol, ad, bd, idesc, (first && p == 1 && kk == kk0) ? 0u : 1u);
+        tc::mma_f16(tmem + dcol, ad, bd, idesc, (first && p == 1 && kk == kk0) ? 0u : 1u);
       }
     }
   }
@@ -684,7 +683,7 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
             const uint32_t idesc = tc::idesc_f16_f32(128, 32 * (S + 1 - p));
 #pragma unroll
             for (int q4 = 0; q4 < 4; ++q4)
-              tc::mma_bf16(acc + (uint32_t)((p - 1) * 32), tc::desc_sw128(a0 + (uint32_t)(p - 1) * 16384u + q4 * 32),
+              tc::mma_f16(acc + (uint32_t)((p - 1) * 32), tc::desc_sw128(a0 + (uint32_t)(p - 1) * 16384u + q4 * 32),
                            tc::desc_sw128(b0 + q4 * 32), idesc, (p == 1 && q4 == 0) ? 0u : 1u);
           }
         }

@@ -790,7 +790,7 @@ __global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A,
       const uint32_t idesc = tc::idesc_bf16_f32(128, 64);
       for (int kk = 0; kk < 4; ++kk) {
         const uint64_t d = tc::desc_sw128(tc::smem_u32(tile) + kk * 32);
-        tc::mma_bf16(tmem, d, d, idesc, (first && kk == 0) ? 0u : 1u);
+        tc::mma_f16(tmem, d, d, idesc, (first && kk == 0) ? 0u : 1u);
       }
       tc::mma_commit(&bar);
     }

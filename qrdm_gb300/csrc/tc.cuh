@@ -3,7 +3,7 @@
 //
 // Conventions used by the kernels of this library:
 //  * operands live in shared memory in the canonical K-major layout with the
-//    128-byte swizzle: a tile of R rows x 64 bf16 (128 B per row), rows
+//    128-byte swizzle: a tile of R rows x 64 16-bit elements (128 B per row), rows
 //    packed, the 16-byte chunk c of row r stored at chunk (c ^ (r & 7));
 //    8-row groups are 1024 B apart (the descriptor's stride offset); tiles
 //    are 1024-byte aligned.
@@ -112,8 +112,10 @@ __host__ __device__ constexpr uint32_t idesc_f16_f32(int M, int N) {
   return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
 }
 
-// D[tmem] (+)= A[smem] * B[smem]^T  (M x K=16 times N x K=16), one thread issues.
-__device__ __forceinline__ void mma_bf16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
+// D[tmem] (+)= A[smem] * B[smem]^T  (M x K=16 times N x K=16), kind::f16 (the
+// operand type, FP16 or BF16 for both, is in the instruction descriptor);
+// one thread issues.
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a_desc, uint64_t b_desc, uint32_t idesc,
                                          uint32_t accumulate) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
@@ -144,7 +146,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 }
 __device__ __forceinline__ void tmem_wait_ld() { asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory"); }
 
-// Byte offset of element (row r, k) in a K-major SW128 bf16 tile of 64 K.
+// Byte offset of element (row r, k) in a K-major SW128 tile of 64 16-bit K elements.
 __device__ __forceinline__ uint32_t sw128_offset(int r, int k) {
   uint32_t chunk = (uint32_t)(k >> 3) ^ (uint32_t)(r & 7);
   return (uint32_t)r * 128u + chunk * 16u + (uint32_t)(k & 7) * 2u;
