@@ -961,12 +961,20 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
         const double vs = sci * S.scal;
         double* xw = W0 + (size_t)i * lda;
         for (int r = i + tid; r < mloc; r += blockDim.x) {
-          if (r == i) {
-            for (int c = i + 1; c < fjb; ++c) W0[(size_t)c * lda + r] -= S.tw[c];
-          } else {
-            const double v = xw[r] * vs;
-            xw[r] = v;
-            for (int c = i + 1; c < fjb; ++c) W0[(size_t)c * lda + r] = fma(-v, S.tw[c], W0[(size_t)c * lda + r]);
+          // eight columns' entries loaded before any is updated and stored
+          // (a store between loads the compiler cannot prove independent
+          // would leave one memory round trip per entry)
+          const double v = r == i ? 0.0 : xw[r] * vs;
+          if (r != i) xw[r] = v;
+          for (int c0 = i + 1; c0 < fjb; c0 += 8) {
+            double e8[8];
+#pragma unroll
+            for (int u = 0; u < 8; ++u) e8[u] = c0 + u < fjb ? W0[(size_t)(c0 + u) * lda + r] : 0.0;
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int c = c0 + u;
+              if (c < fjb) W0[(size_t)c * lda + r] = r == i ? e8[u] - S.tw[c] : fma(-v, S.tw[c], e8[u]);
+            }
           }
         }
         __syncthreads();
