@@ -844,24 +844,29 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
 #undef BMARK
       if (nswap > maxsw) nswap = 0;  // cannot happen: at most 2 nsel + 1 exchanges
       S.nswap = nswap;
-      // composed permutation: first occurrence of each exchanged position
-      int np = 0;
-      for (int e = 0; e < 2 * nswap; ++e) {
-        const int s = e >> 1;
-        const int dst = (e & 1) ? S.swb[s] : S.swa[s];
-        bool keep = true;
-        for (int t = 0; t < s && keep; ++t)
-          if (S.swa[t] == dst || S.swb[t] == dst) keep = false;
-        if (keep && (e & 1) && S.swa[s] == dst) keep = false;
-        if (!keep) continue;
-        int x = dst;
-        for (int t = nswap - 1; t >= 0; --t) {
-          if (x == S.swa[t]) x = S.swb[t];
-          else if (x == S.swb[t]) x = S.swa[t];
-        }
-        if (x != dst) S.perm[np++] = make_int2(dst, x);
+      S.np = 0;
+    }
+    __syncthreads();
+    // composed permutation, one exchange endpoint per thread: the first
+    // occurrence of each exchanged position, its source found by replaying
+    // the exchanges backwards (the entries form a set: their order in
+    // S.perm does not matter, every destination being distinct)
+    for (int e = tid; e < 2 * S.nswap; e += blockDim.x) {
+      const int nswap = S.nswap, s = e >> 1;
+      const int dst = (e & 1) ? S.swb[s] : S.swa[s];
+      bool keep = true;
+#pragma unroll 8
+      for (int t = 0; t < s; ++t)
+        if (S.swa[t] == dst || S.swb[t] == dst) keep = false;
+      if (keep && (e & 1) && S.swa[s] == dst) keep = false;
+      if (!keep) continue;
+      int x = dst;
+#pragma unroll 8
+      for (int t = nswap - 1; t >= 0; --t) {
+        const int a = S.swa[t], b = S.swb[t];
+        x = x == a ? b : (x == b ? a : x);
       }
-      S.np = np;
+      if (x != dst) S.perm[atomicAdd(&S.np, 1)] = make_int2(dst, x);
     }
     __syncthreads();
     const int np = S.np, fjb = S.nsel;
@@ -880,9 +885,20 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
     const int rc = np > 0 ? max(1, min(32, kStage / np)) : 1;
     for (int r0 = 0; r0 < m && np > 0; r0 += rc) {
       double* st = S.stage;
-      for (int e = tid; e < np * rc; e += blockDim.x) {
-        const int t = e / rc, rr = e % rc, r = r0 + rr;
-        if (r < m) st[t * rc + rr] = A[(size_t)(j + S.perm[t].y) * lda + r];
+      // eight loads in flight per thread before their stores to the stage
+      for (int e0 = tid; e0 < np * rc; e0 += 8 * (int)blockDim.x) {
+        double v8[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = e0 + u * (int)blockDim.x;
+          const int t = e / rc, r = r0 + e % rc;
+          v8[u] = (e < np * rc && r < m) ? A[(size_t)(j + S.perm[t].y) * lda + r] : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int e = e0 + u * (int)blockDim.x;
+          if (e < np * rc) st[e] = v8[u];
+        }
       }
       __syncthreads();
       for (int e = tid; e < np * rc; e += blockDim.x) {
