@@ -282,13 +282,16 @@ __device__ __forceinline__ double vval(const double* V0, long long lda, int mloc
   return (a < kc && r < mloc) ? (r > a ? V0[(size_t)a * lda + r] : (r == a ? 1.0 : 0.0)) : 0.0;
 }
 
-// levels of 16 accumulator columns (col .. col + 15) of this thread's lane:
-// hi = sum_{L<=5} D_L 2^(8(5-L)) exact; mid = sum_{L>=6} D_L 2^(8(S+1-L))
-__device__ __forceinline__ void oz_levels16(uint32_t taddr, uint32_t col, long long* hi, long long* mid) {
+// Drain of the levels of 16 accumulator columns (col .. col + 15) of this
+// thread's TMEM lane: hi = sum_{L<=5} D_L 2^(8(5-L)) exactly in int64; the
+// low levels (L >= 6, below the result's rounding) summed in FP32 from the
+// level values, mid = sum_{L>=6} D_L 2^(8(S+1-L)) (no 64-bit integer to
+// float conversion, which runs on the FP64 pipe).
+__device__ __forceinline__ void oz_levels16_drain(uint32_t taddr, uint32_t col, long long* hi, float* mid) {
 #pragma unroll
   for (int j = 0; j < 16; ++j) {
     hi[j] = 0;
-    mid[j] = 0;
+    mid[j] = 0.f;
   }
 #pragma unroll
   for (int L = 2; L <= OZS + 1; ++L) {
@@ -297,11 +300,41 @@ __device__ __forceinline__ void oz_levels16(uint32_t taddr, uint32_t col, long l
     tc::tmem_wait_ld();
 #pragma unroll
     for (int j = 0; j < 16; ++j) {
-      const long long x = (long long)f32_to_int(v[j]);
-      if (L <= 5) hi[j] += x << (8 * (5 - L));
-      else mid[j] += x << (8 * (OZS + 1 - L));
+      if (L <= 5) hi[j] += (long long)f32_to_int(v[j]) << (8 * (5 - L));
+      else mid[j] = fmaf(mid[j], 256.f, v[j]);
     }
   }
+}
+
+// C -= V W2 epilogue (K <= 32, OZS = 7): the levels of 16 columns combined
+// directly, adjacent levels paired exactly in 32-bit integers (|D_L| <=
+// (L-1) 2^19): comb = P1 2^33 + P2 2^17 + P3 2 + (D8 >> 7) with P1 = D2 256 +
+// D3, P2 = D4 256 + D5, P3 = D6 256 + D7 (= hi 2^17 + (mid >> 7)); levels
+// L <= 5 (<= 2^21) converted by the 1.5 2^23 FP32 shifter.
+__device__ __forceinline__ void oz_comb16(uint32_t taddr, uint32_t col, long long* comb) {
+  static_assert(OZS == 7, "paired levels assume 7 digits");
+  int p1[16], p2[16], p3[16], d8[16];
+#pragma unroll
+  for (int L = 2; L <= 8; ++L) {
+    float v[16];
+    tc::tmem_ld16(taddr + (uint32_t)((L - 2) * 32) + col, v);
+    tc::tmem_wait_ld();
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+      const float x = v[j];
+      const int sm = __float_as_int(x + 12582912.0f) - 0x4B400000;  // exact for |x| <= 2^22
+      if (L == 2) p1[j] = sm * 256;
+      else if (L == 3) p1[j] += sm;
+      else if (L == 4) p2[j] = sm * 256;
+      else if (L == 5) p2[j] += sm;
+      else if (L == 6) p3[j] = f32_to_int(x) * 256;
+      else if (L == 7) p3[j] += f32_to_int(x);
+      else d8[j] = f32_to_int(x);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 16; ++j)
+    comb[j] = ((long long)p1[j] << 33) + ((long long)p2[j] << 17) + ((long long)p3[j] << 1) + (long long)(d8[j] >> 7);
 }
 
 // digit-pair MMAs of one operand pair (FP16 digits, digits2_f16): A digits p at a + (p-1) 16 KB, B
@@ -430,12 +463,13 @@ __device__ void cta_vtv_oz(OzCtx& z, const double* V0, long long lda, int mloc, 
     }
     oz_wait(z);
     if ((kb & 3) == 3 || kb == nblk - 1) {
-      long long hi[16], mid[16];
-      oz_levels16(tl, (uint32_t)(16 * ch), hi, mid);
+      long long hi[16];
+      float midf[16];
+      oz_levels16_drain(tl, (uint32_t)(16 * ch), hi, midf);
 #pragma unroll
       for (int j = 0; j < 16; ++j) {
         acc_hi[j] += hi[j];
-        acc_mid[j] += (float)mid[j];
+        acc_mid[j] += midf[j];
       }
     }
     tc::fence_before_sync();
@@ -513,12 +547,13 @@ __device__ void cta_trailing_oz(OzCtx& z, const double* V0, double* C0, long lon
       }
       oz_wait(z);
       if ((kb & 3) == 3 || kb == nblk - 1) {
-        long long hi[16], mid[16];
-        oz_levels16(tl, (uint32_t)(16 * ch), hi, mid);
+        long long hi[16];
+        float midf[16];
+        oz_levels16_drain(tl, (uint32_t)(16 * ch), hi, midf);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           acc_hi[j] += hi[j];
-          acc_mid[j] += (float)mid[j];
+          acc_mid[j] += midf[j];
         }
       }
       tc::fence_before_sync();
@@ -616,17 +651,17 @@ __device__ void cta_trailing_oz(OzCtx& z, const double* V0, double* C0, long lon
         cv[j] = (r < mloc && c < n2) ? C0[(size_t)c * lda + r] : 0.0;
       }
       oz_wait(z);
-      long long hi[16], mid[16];
-      oz_levels16(tl + 256u, (uint32_t)(16 * ch), hi, mid);
+      long long comb[16];
+      oz_comb16(tl + 256u, (uint32_t)(16 * ch), comb);
       if (r < mloc && !z.fail) {
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int c = cw0 + j;
           if (c < n2) {
+            // U = comb 2^(e-57), rounded to FP64 with integer instructions,
+            // then the one FP64 subtraction
             const int e = 1 + wexp[c];  // V scale 2^1 times the W2 column scale
-            constexpr int msh = 8 * (OZS + 1) - 40 - 17;
-            const long long comb = (hi[j] << 17) + (msh >= 0 ? (mid[j] >> msh) : (mid[j] << -msh));
-            C0[(size_t)c * lda + r] = fma(-(double)comb, pow2d(e - 57), cv[j]);
+            C0[(size_t)c * lda + r] = cv[j] - oz_i64_scaled(comb[j], e - 57);
           }
         }
       }
