@@ -72,12 +72,14 @@ def flops_k(m, n, k):
 
 
 def make_matrix_device(name, seed=3):
-    """Column-major workload matrix as a CUDA float64 tensor of shape (n, m)."""
+    """Column-major workload matrix as a float64 tensor of shape (n, m) on
+    the GPU (on the CPU where no GPU exists: the multi-process tests of the
+    reference arm; the low-rank matrix then comes from the CPU generator)."""
     import torch
 
     m, n, _ = WORKLOADS[name]
-    g = torch.Generator(device="cuda").manual_seed(seed)
-    dev = "cuda"
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    g = torch.Generator(device=dev).manual_seed(seed)
     if name == "lowrank16k":
         r = 2048
         lf = torch.randn(m, r, generator=g, dtype=torch.float64, device=dev) / math.sqrt(r)
@@ -162,8 +164,11 @@ def dist_setup(n_gpus):
     if world > 1:
         import torch.distributed as dist
 
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:  # host-only ranks (the tests of the multi-process path)
+            dist.init_process_group("gloo")
     return rank, world, local
 
 
@@ -180,7 +185,7 @@ def max_over_ranks(x, world):
     import torch
     import torch.distributed as dist
 
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
