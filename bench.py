@@ -8,7 +8,7 @@ One step = one DM-QR factorisation of the workload matrix, already resident
 in HBM (restored from a pristine device copy before each step; the copy is
 inside the timed region).  The default workload is the 16384 x 8192
 numerical-rank-2048 matrix A = L R^T + 1e-10 E (full factorisation, nb = 64,
-delta = 0.9, tau_ = 0.15) in the mixed-precision form (Ozaki-split BF16
+delta = 0.9, tau_ = 0.15) in the mixed-precision form (Ozaki-split FP16
 trailing update, BF16 cosine Gram with FP64 recheck).  Inputs (1.07 GB) are
 larger than the 129 MB L2, so no explicit flush is needed between steps.
 
@@ -58,7 +58,7 @@ SELECTION_BASES = {}
 BATCH_COUNT, BATCH_NB = 2000, 32
 BATCH_GENERATOR = None
 BATCH_CPU_SAMPLE = 400
-FP64_PEAK_TFLOPS = 1.25  # nominal dense FP64 of GB300 (no measured FP64 peak)
+FP64_RATES = None
 NB, DELTA, TAU_ = 64, 0.9, 0.15
 CPU_SAMPLE_K = 2048
 
@@ -198,6 +198,30 @@ def load_peaks():
     return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
 
 
+def fp64_rates():
+    """Measured FP64 rates of this GPU in TFLOP/s (the library's
+    qrdm_fp64_rates: independent FMA chains on the CUDA cores, FP64
+    tensor-core MMAs at two shapes), measured once per process."""
+    global FP64_RATES
+    if FP64_RATES is None:
+        from qrdm_gb300 import lib
+
+        out = (C.c_double * 3)()
+        rc = lib().qrdm_fp64_rates(out, 3)
+        FP64_RATES = ({"fma": out[0], "dmma_m8n8k4": out[1], "dmma_m16n8k16": out[2]}
+                      if rc == 0 else {})
+    return FP64_RATES
+
+
+def fp64_peak():
+    """(TFLOP/s, description) of the FP64 roof: the best measured FP64 rate."""
+    r = fp64_rates()
+    if r:
+        best = max(r, key=r.get)
+        return r[best], f"measured ({best}, qrdm_fp64_rates: best of the FMA and FP64 MMA kernels)"
+    return 1.25, "nominal (the FP64 rate measurement failed)"
+
+
 def load_traffic(kernel_key):
     """Per-launch DRAM traffic of a kernel from a committed ncu summary
     (profiles/traffic.txt lines: '<key> <bytes_per_unit> <unit>'), or None."""
@@ -215,9 +239,11 @@ def load_traffic(kernel_key):
     return None
 
 
-def cpu_sample(name, threads, at_host=None):
+def cpu_sample(name, threads, at_host=None, margins=False):
     """Oracle (CPU restatement of the reference, OpenBLAS) on the bounded
-    sample: the workload matrix factored until >= CPU_SAMPLE_K columns."""
+    sample: the workload matrix factored until >= CPU_SAMPLE_K columns.
+    margins=True also records every decision's margin (the oracle's run is
+    then the parity check of the GPU factorisation of the same matrix)."""
     from oracle.oracle import Oracle, run_dmqr
 
     m, n, _ = WORKLOADS[name]
@@ -227,11 +253,46 @@ def cpu_sample(name, threads, at_host=None):
     o = Oracle(threads=threads)
     k_target = min(CPU_SAMPLE_K, min(m, n))
     t0 = time.perf_counter()
-    r = run_dmqr(o, A0, nb=NB, delta=DELTA, tau_=TAU_, kstop=k_target)
+    r = run_dmqr(o, A0, nb=NB, delta=DELTA, tau_=TAU_, kstop=k_target, margins=margins)
     dt = time.perf_counter() - t0
     k = int(np.sum(r["ncols"]))
     f = flops_k(m, n, k) if k < min(m, n) else flops_full(m, n)
-    return {"value": f / dt / 1e12, "seconds": dt, "k": k, "flops": f}
+    return {"value": f / dt / 1e12, "seconds": dt, "k": k, "flops": f, "run": r}
+
+
+def parity_vs_oracle(ref, gpu_jpvt, gpu_ncols, gpu_rdiag, gap=100.0):
+    """The GPU factorisation against the oracle's run of the same matrix
+    (bit-identical to the compiled reference): jpvt and DM block sizes over
+    the oracle's gap-separated prefix (every decision >= gap noise units from
+    its threshold), how far they agree beyond it, and the |R_kk| profile over
+    the columns the oracle factored."""
+    from oracle.oracle import separated_prefix
+
+    pb, pc = separated_prefix(ref, gap)
+    rj, rn = ref["jpvt"], ref["ncols"]
+    kref = int(np.sum(rn))
+    nblk = int(np.count_nonzero(rn))
+    same_blocks = bool(np.array_equal(gpu_ncols[:pb], rn[:pb]))
+    identical = bool(same_blocks and np.array_equal(gpu_jpvt[:pc], rj[:pc]))
+    # leading columns where the two runs made the same choices
+    agree_cols = 0
+    cols = 0
+    for b in range(nblk):
+        if gpu_ncols[b] != rn[b] or not np.array_equal(gpu_jpvt[cols:cols + rn[b]], rj[cols:cols + rn[b]]):
+            break
+        cols += int(rn[b])
+        agree_cols = cols
+    rd_ref = np.abs(np.diag(ref["A"])[:kref])
+    rd_gpu = np.abs(np.asarray(gpu_rdiag)[:kref])
+    ratio = np.where(rd_ref > 0, rd_gpu / np.where(rd_ref > 0, rd_ref, 1.0), 1.0)
+    pre = ratio[:pc] if pc > 0 else ratio[:0]
+    return {"gap_noise_units": gap, "prefix_blocks": int(pb), "prefix_cols": int(pc),
+            "identical": identical, "agree_cols": int(agree_cols),
+            "agree_cols_beyond_prefix": int(max(0, agree_cols - pc)),
+            "oracle_cols": kref, "oracle_blocks": nblk,
+            "rkk_ratio_max_dev_prefix": float(np.max(np.abs(pre - 1.0))) if pre.size else None,
+            "rkk_ratio_max_dev_all": float(np.max(np.abs(ratio - 1.0))) if ratio.size else None,
+            "rkk_ratio_median_dev_all": float(np.median(np.abs(ratio - 1.0))) if ratio.size else None}
 
 
 def run_reference(args):
@@ -264,6 +325,132 @@ def run_reference(args):
             "e2e": {"value": v, "unit": "TFLOP/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
+
+
+def device_backward(L, work, tau, jp, pristine, m, n, k):
+    """||A P - Q R||_F / ||A||_F of a device-resident factorisation (Q R
+    formed by the library's DORMQR applied to R)."""
+    import torch
+
+    Af = work.T
+    R = torch.zeros_like(Af)
+    R[:k, :] = torch.triu(Af[:k, :])
+    if k < min(m, n):
+        R[k:, k:] = Af[k:, k:]
+    QR = R.T.contiguous()
+    del R
+    rq = L.qrdm_dormqr_dev(102, m, n, k, C.c_void_p(work.data_ptr()), m, C.c_void_p(tau.data_ptr()),
+                           C.c_void_p(QR.data_ptr()), m)
+    if rq != 0:
+        return None
+    be = float(torch.linalg.norm(QR - pristine[jp.long() - 1]) / torch.linalg.norm(pristine))
+    del QR
+    return be
+
+
+def single_config(L, stream, name, precisions=("fp64", "mixed"), qp3=False):
+    """One workload of the other configurations, device-resident: one
+    untimed call (workspace growth), then one factorisation per precision
+    timed with CUDA events on the library's stream; backward error of each;
+    the GPU QP3 comparator on the same matrix when asked."""
+    import qrdm_gb300
+    import torch
+
+    from qrdm_gb300 import Stats, default_options
+
+    m, n, desc = WORKLOADS[name]
+    kstop = KSTOP.get(name, 0)
+    pristine = make_matrix_device(name)
+    work = torch.empty_like(pristine)
+    jp = torch.zeros(n, dtype=torch.int32, device="cuda")
+    tau = torch.zeros(min(m, n), dtype=torch.float64, device="cuda")
+    thres = np.array([DELTA, TAU_, 0.0])
+    pd = C.POINTER(C.c_double)
+    out = {"m": m, "n": n, "matrix": desc, "kstop": kstop}
+
+    def run(prec):
+        work.copy_(pristine)
+        jp.zero_()
+        nc = np.zeros(n, np.int32)
+        opt = default_options(precision=qrdm_gb300.PREC[prec], kstop=kstop)
+        st = Stats()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        info = L.dgeqrdm_dev(102, m, n, C.c_void_p(work.data_ptr()), m, C.c_void_p(jp.data_ptr()),
+                             C.c_void_p(tau.data_ptr()), nc.ctypes.data_as(C.POINTER(C.c_int)),
+                             thres.ctypes.data_as(pd), NB, C.byref(opt), C.byref(st))
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), nc, info, st
+
+    for prec in precisions:
+        run(prec)
+        ms, nc, info, st = run(prec)
+        if info != 0:
+            out[prec] = {"info": int(info)}
+            continue
+        k = int(np.sum(nc))
+        F = flops_k(m, n, k) if k < min(m, n) else flops_full(m, n)
+        r = {"ms": ms, "tflops": F / (ms / 1e3) / 1e12, "blocks": int(np.count_nonzero(nc)),
+             "columns": k, "launches": int(st.launches)}
+        if name in SELECTION_BASES:
+            bid = SELECTION_BASES[name]
+            sel = bid[jp[:kstop].cpu().numpy().astype(np.int64) - 1]
+            sel = sel[sel >= 0]
+            r["selected_bases"] = int(len(sel))
+            r["distinct_bases"] = bool(len(np.unique(sel)) == len(sel))
+        r["backward"] = device_backward(L, work, tau, jp, pristine, m, n, min(k, m, n))
+        out[prec] = r
+    if qp3:
+        work.copy_(pristine)
+        jp.zero_()
+        q0 = torch.cuda.Event(enable_timing=True)
+        q1 = torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        rq = L.dgeqp3_dev(102, m, n, C.c_void_p(work.data_ptr()), m, C.c_void_p(jp.data_ptr()),
+                          C.c_void_p(tau.data_ptr()))
+        q1.record(stream)
+        torch.cuda.synchronize()
+        if rq == 0:
+            qms = q0.elapsed_time(q1)
+            out["qp3"] = {"ms": qms, "tflops": flops_full(m, n) / (qms / 1e3) / 1e12,
+                          "backward": device_backward(L, work, tau, jp, pristine, m, n, min(m, n))}
+            if "fp64" in out and "ms" in out["fp64"]:
+                out["fp64_dmqr_over_qp3_speedup"] = qms / out["fp64"]["ms"]
+            if "mixed" in out and "ms" in out["mixed"]:
+                out["mixed_dmqr_over_qp3_speedup"] = qms / out["mixed"]["ms"]
+    if "fp64" in out and "mixed" in out and "ms" in out["fp64"] and "ms" in out["mixed"]:
+        out["mixed_over_fp64_speedup"] = out["fp64"]["ms"] / out["mixed"]["ms"]
+    del pristine, work
+    torch.cuda.empty_cache()
+    return out
+
+
+def other_configs(L, stream):
+    """The other benchmark configurations, one measured step each, for the
+    default run's line: FP64 DM-QR vs QP3 on the 4096^2 Gaussian and Kahan
+    matrices (mixed beside them), the 8192 x 32768 selection stress stopped
+    at 4096 columns, and the 2000-matrix batched launch."""
+    res = {}
+    for name in ("gauss4k", "kahan4k"):
+        try:
+            res[name] = single_config(L, stream, name, qp3=True)
+        except Exception as exc:
+            res[name] = {"error": str(exc)[:200]}
+    try:
+        res["select32k"] = single_config(L, stream, "select32k", precisions=("mixed",))
+    except Exception as exc:
+        res["select32k"] = {"error": str(exc)[:200]}
+    try:
+        bm = batched_measure(L, stream, steps=1, warmup=1)
+        res["batched2000"] = {"matrices_per_s": bm["value"], "ms": bm["ms"], "kernel_ms": bm["kernel_ms"],
+                              "nb": bm["nb"], "precision": bm["precision"], "e2e": bm["e2e"],
+                              "roofline": bm["roofline"], "errors": bm["errors"],
+                              "phase_share": bm["phase_share"]}
+    except Exception as exc:
+        res["batched2000"] = {"error": str(exc)[:200]}
+    return res
 
 
 def run_ours(args):
@@ -344,13 +531,13 @@ def run_ours(args):
             phase["panel_cta0_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames) if nm}
         nblk = int(sti.nblocks)
         if prec == 0:
-            # FP64 FMA GEMMs: no measured FP64 peak exists for this machine;
-            # GB300's nominal dense FP64 rate is used
+            # FP64 GEMMs against the best FP64 rate measured on this GPU
             achieved = sti.trail_flops / (sti.ms_trail / 1e3) / 1e12 if sti.ms_trail > 0 else 0.0
-            roof = {"bound": "tensor", "kernel": "trailing update (k_trail_w_partial + "
-                    "k_trail_w_reduce + k_trail_update), FP64 FMA", "achieved": achieved,
-                    "peak": 1.25, "peak_kind": "nominal FP64 (no measured FP64 peak)",
-                    "unit": "TFLOP/s", "frac": achieved / 1.25,
+            p64, p64_kind = fp64_peak()
+            roof = {"bound": "fp64", "kernel": "trailing update (k_trail_w_partial + "
+                    "k_trail_w_reduce + k_trail_update), FP64", "achieved": achieved,
+                    "peak": p64, "peak_kind": p64_kind,
+                    "unit": "TFLOP/s", "frac": achieved / p64,
                     "traffic": load_traffic("trail_fp64"),
                     "per_launch_basis": f"4 m' n' k flops per DM block, {nblk} blocks"}
         else:
@@ -402,8 +589,12 @@ def run_ours(args):
             roof.update(common)
         # accuracy of the instrumented factorisation, on the device:
         # ||A P - Q R||_F / ||A||_F with Q R formed by the library's DORMQR,
-        # and the |R_kk| profile
+        # ||I - Q^T Q||_F of the economy Q (the library's DORMQR applied to
+        # the first min(m, n) identity columns), and the |R_kk| profile
         accuracy = None
+        gpu_jpvt = jp.cpu().numpy().copy()
+        gpu_ncols = np.array(nc_i, copy=True)
+        gpu_rdiag = torch.abs(torch.diagonal(work.T)[:min(m, n, CPU_SAMPLE_K)]).cpu().numpy()
         try:
             k = int(np.sum(nc_i[:int(np.count_nonzero(nc_i))])) if KSTOP.get(args.workload) else min(m, n)
             k = min(k, m, n)
@@ -413,20 +604,38 @@ def run_ours(args):
             if k < min(m, n):
                 R[k:, k:] = Af[k:, k:]
             QR = R.T.contiguous()  # column-major m x n
+            del R
             rq = L.qrdm_dormqr_dev(102, m, n, k, C.c_void_p(work.data_ptr()), m, C.c_void_p(tau.data_ptr()),
                                    C.c_void_p(QR.data_ptr()), m)
             if rq == 0:
                 p = (jp.long() - 1)
                 be = float(torch.linalg.norm(QR - pristine[p]) / torch.linalg.norm(pristine))
+                del QR
+                mn = min(m, n)
+                qt = torch.zeros((mn, m), dtype=torch.float64, device="cuda")  # column-major m x mn
+                qt[torch.arange(mn, device="cuda"), torch.arange(mn, device="cuda")] = 1.0
+                rq2 = L.qrdm_dormqr_dev(102, m, mn, k, C.c_void_p(work.data_ptr()), m,
+                                        C.c_void_p(tau.data_ptr()), C.c_void_p(qt.data_ptr()), m)
+                orth = None
+                if rq2 == 0:
+                    g = qt @ qt.T  # Q^T Q
+                    g.diagonal().sub_(1.0)
+                    orth = float(torch.linalg.norm(g))
+                    del g
+                del qt
                 rd = torch.abs(torch.diagonal(Af)[:k]).cpu().numpy()
                 r0 = float(rd[0]) if rd.size else 0.0
                 accuracy = {"backward": be, "backward_bound_10_n_eps": 10 * max(m, n) * 2.0 ** -53,
+                            "orth": orth, "orth_bound_100_n_eps": 100 * max(m, n) * 2.0 ** -53,
+                            "orth_basis": f"||I - Q^T Q||_F of the economy Q (m x {min(m, n)})",
                             "rkk_first": r0, "rkk_at": {str(i): float(rd[i]) for i in
                                                         (min(k - 1, 2047), min(k - 1, 2048), k - 1)},
                             "numerical_rank_1e-8": int(np.count_nonzero(rd > 1e-8 * r0))}
-            del R, QR
+            else:
+                del QR
         except Exception as exc:  # accuracy is reported, never fatal for the timing
             accuracy = {"error": str(exc)[:200]}
+        torch.cuda.empty_cache()
         # e2e through the host C ABI with pinned host buffers
         a_host = torch.empty((n, m), dtype=torch.float64, pin_memory=True)
         a_host.copy_(pristine)
@@ -488,14 +697,25 @@ def run_ours(args):
                 variants["speedup_vs_fp64"] = variants["fp64_dmqr_ms"] / ms
             variants["phase_ms"] = phase
             variants["blocks"] = nblk
+            variants["fp64_rates_tflops"] = fp64_rates()
+            if args.workload == "lowrank16k" and args.configs:
+                variants["configs"] = other_configs(L, stream)
         cpu = None
         if args.cpu_baseline:
             threads = os.cpu_count() or 1
-            s = cpu_sample(args.workload, threads, pristine.cpu().numpy())
+            s = cpu_sample(args.workload, threads, pristine.cpu().numpy(), margins=True)
             cpu = {"value": s["value"], "unit": "TFLOP/s", "cores": threads, "kind": "port",
                    "sample": f"{args.workload} factored until >= {CPU_SAMPLE_K} columns "
                              f"(k={s['k']}, {s['seconds']:.1f} s), oracle port of the reference "
                              "on OpenBLAS, all host threads"}
+            # the same oracle run pins the GPU factorisation's choices
+            try:
+                par = parity_vs_oracle(s["run"], gpu_jpvt, gpu_ncols, gpu_rdiag)
+            except Exception as exc:
+                par = {"error": str(exc)[:200]}
+            if accuracy is None or "error" in accuracy:
+                accuracy = {"error": (accuracy or {}).get("error")}
+            accuracy["parity"] = par
         out = {"metric": "DM-QR effective FP64 TFLOP/s", "value": value, "unit": "TFLOP/s",
                "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
@@ -558,12 +778,43 @@ def batched_setup(seed=4, count=None):
     return b, shapes
 
 
-def batched_roofline_s(shapes, bw_gbs):
-    """Summed roofline time: each problem at max(flops / FP64 peak, bytes / BW)."""
-    t = 0.0
-    for m, n in shapes:
-        t += max(flops_full(m, n) / (FP64_PEAK_TFLOPS * 1e12), 16.0 * m * n / (bw_gbs * 1e9))
-    return t
+OZ_PRODUCTS_BATCHED = 28  # digit products per FP64 MAC in the batched kernel (7 digits, levels <= 8)
+
+
+def batched_roofline(shapes, ncols_all, v_off, mixed, p64, ptc, bw):
+    """Summed per-problem roofline of the batched launch, on the arithmetic
+    each phase actually uses, from the DM block sizes the run produced
+    (problem i's blocks k_1, k_2, ... at column j with m' = m - j, n' = n - j):
+      FP64 pipe: the panel 2 m' k^2 - 2 k^3 / 3, the T recurrence k^3 / 3,
+        W2 = T^T W k^2 (n' - k), the norm downdate 2 k (n' - k); in the FP64
+        form also the products below;
+      tensor pipe (mixed form): the trailing update 4 m' (n' - k) k and V^T V
+        m' k^2, each as 28 FP16 digit products, and the BF16 cosine Gram
+        2 m' k^2 (k candidates at least);
+      HBM: 16 m n bytes (the matrix read and written once).
+    Problem time = max(FP64 / P64, tensor / Ptc, bytes / BW); returns
+    (sum of problem times in s, FP64 flops, tensor flops)."""
+    t = f64_all = ftc_all = 0.0
+    for i, (m, n) in enumerate(shapes):
+        blocks = np.asarray(ncols_all[int(v_off[i]):int(v_off[i + 1])], dtype=np.float64)
+        blocks = blocks[blocks > 0]
+        a64 = atc = 0.0
+        j = 0.0
+        for kb in blocks:
+            mp, nn = m - j, n - j
+            rest = max(0.0, nn - kb)
+            a64 += 2.0 * mp * kb * kb - 2.0 * kb ** 3 / 3.0 + kb ** 3 / 3.0 + kb * kb * rest + 2.0 * kb * rest
+            prod = 4.0 * mp * rest * kb + mp * kb * kb
+            gram = 2.0 * mp * kb * kb
+            if mixed:
+                atc += OZ_PRODUCTS_BATCHED * prod + gram
+            else:
+                a64 += prod + gram
+            j += kb
+        t += max(a64 / (p64 * 1e12), atc / (ptc * 1e12), 16.0 * m * n / (bw * 1e9))
+        f64_all += a64
+        ftc_all += atc
+    return t, f64_all, ftc_all
 
 
 def batched_errors(b, pristine):
@@ -607,23 +858,19 @@ def batched_cpu_sample(b_shapes, pristine_host, offs, threads, seed=7, nb=BATCH_
     return {"value": len(mats) / dt, "seconds": dt, "problems": len(mats)}
 
 
-def run_batched(args):
+def batched_measure(L, stream, steps, warmup, count=None, batch_nb=0, precision="mixed",
+                    cpu_baseline=False, world=1, clocks=False, local=0):
+    """The batched workload: one step = one persistent launch factoring the
+    whole batch (device-resident, restored from a pristine copy inside the
+    timed region).  Returns the measurement dict (rank-local timing)."""
     import torch
 
-    from qrdm_gb300 import lib
-
-    rank, world, local = dist_setup(args.gpus)
-    torch.cuda.set_device(local)
-    L = lib()
-    stream = torch.cuda.current_stream()
-    L.qrdm_set_stream(C.c_void_p(stream.cuda_stream))
-    b, shapes = batched_setup(count=args.count)
-    count = len(shapes)
+    b, shapes = batched_setup(count=count)
+    n_prob = len(shapes)
     pristine = b.a.clone()
-    launches_per_step = 1
     tuned = None
-    if args.batch_nb > 0:
-        bnb, bprec = args.batch_nb, args.precision
+    if batch_nb > 0:
+        bnb, bprec = batch_nb, precision
     else:
         # block size and arithmetic from the autotuner (timed on a sample of
         # the batch's shapes)
@@ -638,103 +885,135 @@ def run_batched(args):
         if r != 0:
             raise RuntimeError(f"dgeqrdm_batched_dev returned {r}")
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         step()
     torch.cuda.synchronize()
     barrier(world)
-    with ClockSampler(local) as clk:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
+    clk = ClockSampler(local) if clocks else None
+    if clk:
+        clk.__enter__()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    barrier(world)
+    ev0.record(stream)
+    for _ in range(steps):
+        step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    if clk:
+        clk.__exit__()
+    ms = max_over_ranks(ev0.elapsed_time(ev1) / steps, world)
+    out = {"ms": ms, "count": n_prob, "nb": bnb, "precision": bprec, "autotune": tuned,
+           "value": world * n_prob / (ms / 1e3), "clocks": clk.summary() if clk else None}
+    peaks, peak_kind = load_peaks()
+    F = sum(flops_full(m, n) for m, n in shapes)
+    # kernel-only time of the persistent launch (events around the run)
+    b.a.copy_(pristine)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    b.run(nb=bnb, delta=DELTA, tau_=TAU_, precision=bprec)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    kms = e0.elapsed_time(e1)
+    cyc = (C.c_ulonglong * 9)()
+    L.qrdm_batched_phase_cycles(cyc, 9)
+    names = ["norms", "select", "panel", "tfactor", "trail", "downdate", "queue"]
+    busy = float(cyc[7]) or 1.0
+    phases = {nm: float(cyc[k]) / busy for k, nm in enumerate(names)}
+    nsm = torch.cuda.get_device_properties(local).multi_processor_count
+    phases["longest_over_mean_cta"] = float(cyc[8]) / (busy / nsm)
+    p64, p64_kind = fp64_peak()
+    ptc = peaks.get("bf16_tflops")
+    nc_all = b.ncols.cpu().numpy()
+    t_roof, f64, ftc = batched_roofline(shapes, nc_all, b.v_off, bprec == "mixed", p64, ptc,
+                                        peaks["hbm_gbs"])
+    try:
+        be, orth = batched_errors(b, pristine)
+    except RuntimeError:  # torch's GPU linear algebra unavailable
+        be, orth = np.full(1, np.nan), np.full(1, np.nan)
+    out["roofline"] = {
+        "bound": "summed per-problem roof (FP64 pipe, tensor pipe, HBM)",
+        "kernel": "k_dmqr_batched (one persistent launch; trailing update, V^T V and Gram on " +
+                  ("FP16/BF16 tensor cores" if bprec == "mixed" else "the FP64 pipe") + ")",
+        "achieved": n_prob / (kms / 1e3), "peak": n_prob / t_roof, "unit": "matrices/s",
+        "frac": t_roof / (kms / 1e3),
+        "peaks": {"fp64_tflops": p64, "fp64_kind": p64_kind, "tensor_tflops": ptc,
+                  "tensor_kind": f"{peak_kind} bf16 burst (FP16 rate equal)",
+                  "hbm_gbs": peaks["hbm_gbs"]},
+        "fp64_flops": f64, "tensor_flops": ftc, "fp64_equivalent_flops": F,
+        "effective_fp64_tflops": F / (kms / 1e3) / 1e12,
+        "traffic": load_traffic("dmqr_batched"),
+        "per_launch_basis": f"{n_prob} problems; per problem max(FP64 work / P64, tensor work / "
+                            "Ptc, 16 m n B / BW) over its actual DM blocks"}
+    out["kernel_ms"] = kms
+    out["phase_share"] = phases
+    out["errors"] = {"backward_p50": float(np.percentile(be, 50)),
+                     "backward_p99": float(np.percentile(be, 99)),
+                     "backward_max": float(be.max()),
+                     "orth_p50": float(np.percentile(orth, 50)),
+                     "orth_p99": float(np.percentile(orth, 99))}
+    # e2e: pinned host buffer -> device, factor, factors back to the host
+    host = torch.empty(pristine.numel(), dtype=torch.float64, pin_memory=True)
+    host.copy_(pristine)
+    back = torch.empty_like(host)
+    e2e_t = []
+    for _ in range(2):
         torch.cuda.synchronize()
-        barrier(world)
-        ev0.record(stream)
-        for _ in range(args.steps):
-            step()
-        ev1.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-    ms = max_over_ranks(ev0.elapsed_time(ev1) / args.steps, world)
-    value = world * count / (ms / 1e3)
-    clocks = clk.summary()
-    if rank == 0:
-        peaks, peak_kind = load_peaks()
-        F = sum(flops_full(m, n) for m, n in shapes)
-        t_roof = batched_roofline_s(shapes, peaks["hbm_gbs"])
-        # kernel-only time of the persistent launch (events around the run)
-        b.a.copy_(pristine)
-        e0 = torch.cuda.Event(enable_timing=True)
-        e1 = torch.cuda.Event(enable_timing=True)
-        e0.record(stream)
+        t0 = time.perf_counter()
+        b.a.copy_(host, non_blocking=True)
         b.run(nb=bnb, delta=DELTA, tau_=TAU_, precision=bprec)
-        e1.record(stream)
+        back.copy_(b.a, non_blocking=True)
+        b.jpvt.cpu()
+        b.tau.cpu()
         torch.cuda.synchronize()
-        kms = e0.elapsed_time(e1)
-        cyc = (C.c_ulonglong * 9)()
-        L.qrdm_batched_phase_cycles(cyc, 9)
-        names = ["norms", "select", "panel", "tfactor", "trail", "downdate", "queue"]
-        busy = float(cyc[7]) or 1.0
-        phases = {nm: float(cyc[k]) / busy for k, nm in enumerate(names)}
-        nsm = torch.cuda.get_device_properties(local).multi_processor_count
-        phases["longest_over_mean_cta"] = float(cyc[8]) / (busy / nsm)
-        try:
-            be, orth = batched_errors(b, pristine)
-        except RuntimeError:  # torch's GPU linear algebra unavailable
-            be, orth = np.full(1, np.nan), np.full(1, np.nan)
-        achieved = F / (kms / 1e3) / 1e12
-        roof = {"bound": "fp64", "kernel": "k_dmqr_batched (one persistent launch; trailing update "
-                "on " + ("BF16 tensor cores, Ozaki split" if bprec == "mixed" else "FP64") + ")",
-                "achieved": achieved, "peak": FP64_PEAK_TFLOPS,
-                "peak_kind": "nominal FP64 (no measured FP64 peak); HBM term from measured "
-                             f"{peaks['hbm_gbs']} GB/s", "unit": "TFLOP/s",
-                "frac": t_roof / (kms / 1e3),
-                "summed_roofline_mats_per_s": count / t_roof,
-                "traffic": load_traffic("dmqr_batched"),
-                "per_launch_basis": "sum_i 2 m_i n_i^2 - 2 n_i^3 / 3 flops over 2000 problems"}
-        # e2e: pinned host buffer -> device, factor, factors back to the host
-        host = torch.empty(pristine.numel(), dtype=torch.float64, pin_memory=True)
-        host.copy_(pristine)
-        back = torch.empty_like(host)
-        e2e_t = []
-        for _ in range(2):
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            b.a.copy_(host, non_blocking=True)
-            b.run(nb=bnb, delta=DELTA, tau_=TAU_, precision=bprec)
-            back.copy_(b.a, non_blocking=True)
-            jp_h = b.jpvt.cpu()
-            tau_h = b.tau.cpu()
-            torch.cuda.synchronize()
-            e2e_t.append(time.perf_counter() - t0)
-        h2d = 8 * pristine.numel()
-        d2h = 8 * pristine.numel() + 4 * b.jpvt.numel() + 8 * b.tau.numel()
-        e2e = {"value": world * count / min(e2e_t), "unit": "matrices/s",
-               "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
-        cpu = None
-        if args.cpu_baseline:
-            threads = os.cpu_count() or 1
-            s = batched_cpu_sample(shapes, pristine.cpu().numpy(), b.a_off, threads, nb=bnb)
-            cpu = {"value": s["value"], "unit": "matrices/s", "cores": threads, "kind": "port",
-                   "sample": f"{s['problems']} problems of the batch drawn by seed, factored one "
-                             f"after another by the oracle port on OpenBLAS ({s['seconds']:.1f} s)"}
-        out = {"metric": "batched DM-QR matrices/s", "value": value, "unit": "matrices/s",
-               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
+        e2e_t.append(time.perf_counter() - t0)
+    h2d = 8 * pristine.numel()
+    d2h = 8 * pristine.numel() + 4 * b.jpvt.numel() + 8 * b.tau.numel()
+    out["e2e"] = {"value": world * n_prob / min(e2e_t), "unit": "matrices/s",
+                  "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
+    out["flops"] = F
+    out["bytes"] = 8 * pristine.numel()
+    out["cpu"] = None
+    if cpu_baseline:
+        threads = os.cpu_count() or 1
+        sc = batched_cpu_sample(shapes, pristine.cpu().numpy(), b.a_off, threads, nb=bnb)
+        out["cpu"] = {"value": sc["value"], "unit": "matrices/s", "cores": threads, "kind": "port",
+                      "sample": f"{sc['problems']} problems of the batch drawn by seed, factored one "
+                                f"after another by the oracle port on OpenBLAS ({sc['seconds']:.1f} s)"}
+    del b, pristine, host, back
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_batched(args):
+    import torch
+
+    from qrdm_gb300 import lib
+
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    L = lib()
+    stream = torch.cuda.current_stream()
+    L.qrdm_set_stream(C.c_void_p(stream.cuda_stream))
+    r = batched_measure(L, stream, args.steps, args.warmup, count=args.count, batch_nb=args.batch_nb,
+                        precision=args.precision, cpu_baseline=args.cpu_baseline and rank == 0,
+                        world=world, clocks=True, local=local)
+    if rank == 0:
+        out = {"metric": "batched DM-QR matrices/s", "value": r["value"], "unit": "matrices/s",
+               "n_gpus": world, "steps": args.steps, "warmup": args.warmup, "ms_per_step": r["ms"],
                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                "data": "synthetic",
-               "config": {"workload": "batched2000", "count": count, "nb": bnb,
-                          "precision": bprec, "autotune": tuned,
-                          "delta": DELTA, "tau_": TAU_, "flops": F, "generator": BATCH_GENERATOR,
-                          "bytes": 8 * pristine.numel(),
-                          "parallelism": f"replicas{world}",
+               "config": {"workload": "batched2000", "count": r["count"], "nb": r["nb"],
+                          "precision": r["precision"], "autotune": r["autotune"],
+                          "delta": DELTA, "tau_": TAU_, "flops": r["flops"], "generator": BATCH_GENERATOR,
+                          "bytes": r["bytes"], "parallelism": f"replicas{world}",
                           "l2": "inputs (3.3 GB) larger than L2; no flush needed"},
-               "roofline": roof, "cpu_baseline": cpu, "e2e": e2e,
-               "gpu_launches": launches_per_step * args.steps, "clocks": clocks,
-               "phase_share": phases,
-               "errors": {"backward_p50": float(np.percentile(be, 50)),
-                          "backward_p99": float(np.percentile(be, 99)),
-                          "backward_max": float(be.max()),
-                          "orth_p50": float(np.percentile(orth, 50)),
-                          "orth_p99": float(np.percentile(orth, 99)),
-                          "kernel_ms": kms}}
+               "roofline": r["roofline"], "cpu_baseline": r["cpu"], "e2e": r["e2e"],
+               "gpu_launches": args.steps, "clocks": r["clocks"],
+               "phase_share": r["phase_share"], "errors": {**r["errors"], "kernel_ms": r["kernel_ms"]}}
         print(json.dumps(out), flush=True)
     barrier(world)
     if world > 1:
@@ -783,6 +1062,8 @@ def main():
     ap.add_argument("--workload", choices=sorted(WORKLOADS), default="lowrank16k")
     ap.add_argument("--precision", choices=["mixed", "fp64"], default="mixed")
     ap.add_argument("--no-variants", dest="variants", action="store_false")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="default workload: skip the one-step measurements of the other configurations")
     ap.add_argument("--count", type=int, default=None,
                     help="batched2000: number of problems (default 2000)")
     ap.add_argument("--slices", type=int, default=0,

@@ -34,7 +34,7 @@ extern "C" {
 
 /* Arithmetic of the trailing update (the dominant cost). */
 #define QRDM_PREC_FP64 0  /* native FP64 everywhere                           */
-#define QRDM_PREC_MIXED 1 /* Ozaki-split FP64 emulation on BF16 tensor cores  */
+#define QRDM_PREC_MIXED 1 /* Ozaki-split FP64 emulation on FP16 tensor cores  */
 
 typedef struct qrdm_options {
   int precision;      /* QRDM_PREC_FP64 (default) or QRDM_PREC_MIXED             */
@@ -43,7 +43,11 @@ typedef struct qrdm_options {
   int slices;         /* Ozaki slices per operand, 4..7 (0 = default 7)          */
   double gram_margin; /* mixed Gram: |cos| within this of delta is recomputed in
                          FP64 (0 = default)                                      */
-  int reserved[8];
+  int wait_limit;     /* > 0: polls after which a device-wide wait (the panels'
+                         grid barriers) gives up and the call returns
+                         QRDM_ERR_TIMEOUT; capped at, and 0 = the default, 2^26.
+                         A small value is a test hook for the timeout path.     */
+  int reserved[7];
 } qrdm_options;
 
 typedef struct qrdm_stats {
@@ -94,18 +98,23 @@ int dgeqrdm_dev(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jp
                 int* ncols, const double* thres, int nb, const qrdm_options* opt,
                 qrdm_stats* stats);
 
-/* dgeqrdm_dev for callers that cannot allocate device memory (inside a
- * stream capture or a real-time loop where cudaMalloc would synchronise or
- * fail, or inside a host application that owns every allocation).  No
- * counterpart in the reference.  Allocates nothing: all scratch lives in one
- * fixed 10 MiB device array inside the library, so problems are limited to
- * m <= 1024, n <= 1024, nb <= 64 (larger sizes return QRDM_ERR_UNSUPPORTED
- * with a message on stderr).  Options are the defaults (FP64, NaN scan).
- * a, jpvt, tau are device pointers, ncols and thres host pointers; `stream`
- * is a cudaStream_t (NULL: the legacy default stream).  The first call on a
- * device looks up the array's device address and sets kernel attributes;
- * make that first call before any stream capture.  Every call shares the
- * array: calls that overlap on the GPU race and corrupt each other. */
+/* dgeqrdm_dev for callers that cannot allocate device memory: plug-ins
+ * whose host application owns every device allocation (a pool or arena the
+ * plug-in may not grow), real-time loops where cudaMalloc/cudaFree would
+ * stall on an implicit device synchronisation, and processes that run at
+ * their memory limit.  No counterpart in the reference.  Allocates nothing:
+ * all scratch lives in one fixed 10 MiB device array inside the library, so
+ * problems are limited to m <= 1024, n <= 1024, nb <= 64 (larger sizes
+ * return QRDM_ERR_UNSUPPORTED with a message on stderr).  Options are the
+ * defaults (FP64, NaN scan).  a, jpvt, tau are device pointers, ncols and
+ * thres host pointers; `stream` is a cudaStream_t (NULL: the legacy default
+ * stream).  The call synchronises that stream with the host once per DM
+ * block (the host reads the block's size back to place the next one) and
+ * twice more when jpvt marks fixed columns, so it must not be issued on a
+ * stream that is being captured into a CUDA graph.  The first call on a
+ * device looks up the array's device address and sets kernel attributes.
+ * Every call shares the array: calls that overlap on the GPU race and
+ * corrupt each other. */
 int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda, int* d_jpvt,
                         double* d_tau, int* ncols, const double* thres, int nb, void* stream);
 
@@ -121,7 +130,7 @@ int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda, i
  *           d_info count ints (0 or -13) or NULL.
  * thres = [delta, tau_, eta] (host), stop = the stop mode of dgeqrdm's
  * ncols[0] (0..3) for every problem, nb <= 64.  precision: 0 = FP64, 1 =
- * trailing update on the BF16 tensor cores with the Ozaki split (FP64
+ * trailing update on the FP16 tensor cores with the Ozaki split (FP64
  * accuracy; nb <= 32).  Repeated calls with the same description replay a
  * captured CUDA graph. */
 int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int* d_jpvt, double* d_tau,
@@ -140,6 +149,14 @@ int qrdm_batched_phase_cycles(unsigned long long* out, int nout);
  * additions, kernel lifetime.
  * Instrumentation only (no counterpart in the reference). */
 int qrdm_panel_phase_cycles(unsigned long long* out, int nout);
+
+/* Measured FP64 rates of the current GPU in TFLOP/s: out[0] = FMA on the
+ * CUDA cores, out[1] = FP64 tensor-core MMA (mma.sync m8n8k4), out[2] =
+ * FP64 tensor-core MMA (m16n8k16); each from a kernel of independent chains
+ * that fills every SM, best of three timed launches.  The denominators of
+ * the FP64 rooflines.  Instrumentation only (no counterpart in the
+ * reference); synchronises the device. */
+int qrdm_fp64_rates(double* out, int nout);
 
 /* ------------------------------------------------------------------ QP3 */
 /* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot

@@ -10,10 +10,14 @@
 # reference's unprefixed names onto them.  Sources are compiled where they lie
 # (read-only), outputs go to oracle/_ref/ only.
 #
-# Usage: oracle/build_ref.sh [reference_root]   (default /root/reference)
+# Usage: oracle/build_ref.sh <reference_root>   (or QRDM_REFERENCE_ROOT in the environment)
 set -euo pipefail
 HERE="$(cd "$(dirname "$0")" && pwd)"
-REF="${1:-/root/reference}"
+REF="${1:-${QRDM_REFERENCE_ROOT:-}}"
+if [ -z "$REF" ]; then
+  echo "build_ref: no reference root given (argument or QRDM_REFERENCE_ROOT); skipping" >&2
+  exit 0
+fi
 OUT="$HERE/_ref"
 if [ ! -d "$REF/src" ]; then
   echo "build_ref: reference sources not found at $REF; skipping" >&2

@@ -23,7 +23,7 @@
  * identical BLAS calls in identical order the oracle reproduces the compiled
  * reference bit for bit (pinned by tests/test_oracle.py).
  *
- * Deliberate differences from the reference, all documented in the design doc:
+ * Deliberate differences from the reference:
  *  - the norm sort is an explicit stable merge sort on (norm desc, index asc);
  *    glibc's qsort (used by the reference) is a stable merge sort for these
  *    sizes, so the order is the same;

@@ -61,22 +61,30 @@ def build_oracle(force: bool = False) -> str:
     return ORACLE_SO
 
 
-# where build_ref.sh finds the reference sources (present only in the
-# container that holds them; never on the GPU machine)
-REFERENCE_ROOT = os.environ.get("QRDM_REFERENCE_ROOT", "/root/reference")
+def reference_root(root: str | None = None) -> str | None:
+    """Root of the reference sources: the argument, else the environment
+    variable QRDM_REFERENCE_ROOT; None when neither is given."""
+    return root or os.environ.get("QRDM_REFERENCE_ROOT") or None
 
 
-def reference_sources_present() -> bool:
-    return os.path.isdir(os.path.join(REFERENCE_ROOT, "src"))
+def reference_sources_present(root: str | None = None) -> bool:
+    r = reference_root(root)
+    return bool(r) and os.path.isdir(os.path.join(r, "src"))
 
 
-def build_reference() -> str | None:
-    """Compile the unmodified reference sources (only where they exist)."""
-    script = os.path.join(HERE, "build_ref.sh")
-    if not reference_sources_present():
-        return None
-    subprocess.check_call(["bash", script, REFERENCE_ROOT])
-    return REF_SO if os.path.exists(REF_SO) else None
+def reference_built() -> bool:
+    """True once build_ref.sh has produced the compiled reference."""
+    return os.path.exists(REF_SO)
+
+
+def build_reference(root: str | None = None) -> str | None:
+    """Compile the unmodified reference sources found under ``root`` (or
+    QRDM_REFERENCE_ROOT); nothing happens where they are absent."""
+    r = reference_root(root)
+    if not reference_sources_present(r):
+        return REF_SO if reference_built() else None
+    subprocess.check_call(["bash", os.path.join(HERE, "build_ref.sh"), r])
+    return REF_SO if reference_built() else None
 
 
 def _dp(a):

@@ -18,7 +18,7 @@ class Options(C.Structure):
     """struct qrdm_options."""
     _fields_ = [("precision", C.c_int), ("kstop", C.c_int), ("nancheck", C.c_int),
                 ("slices", C.c_int), ("gram_margin", C.c_double),
-                ("reserved", C.c_int * 8)]
+                ("wait_limit", C.c_int), ("reserved", C.c_int * 7)]
 
 
 class Stats(C.Structure):
@@ -47,6 +47,7 @@ SIGNATURES = {
                                       C.c_void_p, C.c_void_p, _pd, C.c_int, C.c_int, C.c_int]),
     "qrdm_batched_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     "qrdm_panel_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
+    "qrdm_fp64_rates": (C.c_int, [_pd, C.c_int]),
     "dgeqp3": (C.c_int, [C.c_int, C.c_int, C.c_int, _pd, C.c_int, _pi, _pd]),
     "dgeqp3_dev": (C.c_int, [C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p,
                              C.c_void_p]),

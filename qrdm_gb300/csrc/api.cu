@@ -100,6 +100,7 @@ struct DmqrProblem {
   int slices = 7;  // Ozaki digits per operand (mixed precision)
   double gram_margin = 0.0078125;  // mixed Gram: FP64 recheck band around delta
   int nfxd = 0;    // fixed leading columns already factored
+  unsigned spin_limit = QRDM_SPIN_LIMIT;  // polls before a device-wide wait gives up
 };
 
 #define RET(x)                 \
@@ -461,6 +462,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       pa.allow_exit = 1;
       pa.skip_vtv = oz_block ? 1 : 0;
       pa.prof = timing ? c.pan_prof.as<unsigned long long>() : nullptr;
+      pa.spin_limit = P.spin_limit;
       RET(launch_panel(c, pa, mloc, kmax, s, &G));
     }
     PH(2);
@@ -593,6 +595,8 @@ int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, i
   P.slices = o.slices == 0 ? 7 : o.slices;
   P.gram_margin = o.gram_margin > 0.0 ? o.gram_margin : 0.0078125;
   if (P.slices < 4 || P.slices > 7) return -1;
+  if (o.wait_limit < 0) return -1;
+  if (o.wait_limit > 0) P.spin_limit = (unsigned)std::min<long long>(o.wait_limit, QRDM_SPIN_LIMIT);
   cudaStream_t s = c.stream();
   std::vector<int> hv;
   int* hj = hj_buf;
@@ -656,6 +660,7 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
     pa.allow_exit = 0;
     pa.skip_vtv = 0;
     pa.prof = nullptr;
+    pa.spin_limit = QRDM_SPIN_LIMIT;
     RET(launch_panel(c, pa, mloc, kb, s, &G));
     int npair = kb * (kb - 1) / 2;
     k_vtv_reduce<<<std::max(1, ceil_div(8 * npair, 256)), 256, 0, s>>>(c.vtv_part.as<double>(), G, d_st, c.vtv.as<double>());

@@ -72,7 +72,8 @@ __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, doub
 // --------------------------------------------------- bounded grid barrier
 // Monotonic-counter barrier for cooperative launches: every CTA arrives
 // once per barrier; barrier b completes when the counter reaches
-// nblocks * (b + 1).  The spin is bounded: on timeout the CTA sets
+// nblocks * (b + 1).  The spin is bounded (`limit` polls, QRDM_SPIN_LIMIT
+// unless the caller asked for fewer): on timeout the CTA sets
 // QRDM_EDEV_BARRIER_TIMEOUT and returns false so the kernel can unwind.
 #ifndef QRDM_SPIN_LIMIT
 #define QRDM_SPIN_LIMIT (1u << 26)
@@ -86,7 +87,8 @@ __device__ __forceinline__ void red_release_add_u32(unsigned* p, unsigned v) {
   asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err) {
+__device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target, int* err,
+                                             unsigned limit) {
   __syncthreads();
   __shared__ int s_ok;
   if (threadIdx.x == 0) {
@@ -95,7 +97,7 @@ __device__ __forceinline__ bool grid_barrier(unsigned* counter, unsigned target,
     unsigned spins = 0;
     int ok = 1;
     while (ld_acquire_u32(counter) < target) {
-      if (++spins > QRDM_SPIN_LIMIT || (*(volatile int*)err & QRDM_EDEV_BARRIER_TIMEOUT)) {
+      if (++spins > limit || (*(volatile int*)err & QRDM_EDEV_BARRIER_TIMEOUT)) {
         atomicOr(err, QRDM_EDEV_BARRIER_TIMEOUT);
         ok = 0;
         break;

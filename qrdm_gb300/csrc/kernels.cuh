@@ -32,6 +32,7 @@ struct PanelArgs {  // every field is set by the launching code
   int allow_exit;     // 1: DM early exit (dgeqr2_mia); 0: plain dgeqr2
   int skip_vtv;       // 1: leave the V^T V partials to the caller (mixed precision)
   unsigned long long* prof;  // k_panel_red: CTA 0's per-phase cycles [8] (added to), or null
+  unsigned spin_limit;       // polls before a grid barrier gives up (QRDM_SPIN_LIMIT by default)
 };
 
 struct TrailArgs {

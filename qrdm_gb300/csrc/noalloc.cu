@@ -1,13 +1,15 @@
 // noalloc.cu -- DM-QR entry point that allocates no memory.
 //
 // Some callers cannot call cudaMalloc at the point where they factor a
-// matrix: code running inside a CUDA graph capture or a real-time loop
-// where an allocation would synchronise the device or fail, plug-ins whose
-// host application owns every device allocation, and processes that run at
-// their memory limit.  dgeqrdm_dev_noalloc serves them: every piece of
-// scratch memory it needs lives in one file-scope __device__ array of fixed
-// size (held by every GPU that loads the library until the process exits);
-// the caller still passes the matrix, jpvt and tau in device memory.
+// matrix: plug-ins whose host application owns every device allocation,
+// real-time loops where an allocation would stall on an implicit device
+// synchronisation, and processes that run at their memory limit.
+// dgeqrdm_dev_noalloc serves them: every piece of scratch memory it needs
+// lives in one file-scope __device__ array of fixed size (held by every GPU
+// that loads the library until the process exits); the caller still passes
+// the matrix, jpvt and tau in device memory.  The call reads each DM block's
+// size back to the host (a stream synchronisation per block), so it cannot
+// be recorded into a CUDA graph.
 //
 // The array is shared by all calls: two calls that overlap on the GPU (for
 // example on two streams) race on it and corrupt each other's results.
@@ -105,6 +107,10 @@ using namespace qrdm;
 extern "C" int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a, int lda,
                                    int* d_jpvt, double* d_tau, int* ncols, const double* thres,
                                    int nb, void* stream) {
+  // invalid shapes are rejected before any workspace is touched (the
+  // argument checks of dgeqrdm give -1 for them as well), so no path reaches
+  // a buffer that is not a view into the static array
+  if (m <= 0 || n <= 0 || nb <= 0 || !thres || !ncols) return -1;
   if (m > kNoallocMaxM || n > kNoallocMaxN || nb > kNoallocMaxNb) {
     fprintf(stderr,
             "dgeqrdm_dev_noalloc: m=%d n=%d nb=%d exceeds the static scratch "
@@ -118,7 +124,7 @@ extern "C" int dgeqrdm_dev_noalloc(int matrix_layout, int m, int n, double* d_a,
   int r = noalloc_setup(dev);
   if (r) return r;
   NoallocDevice& d = g_na[dev];
-  if (m > 0 && n > 0 && nb > 0 && !carve(d, m, n, nb)) {
+  if (!carve(d, m, n, nb)) {
     fprintf(stderr, "dgeqrdm_dev_noalloc: workspace for m=%d n=%d nb=%d exceeds %zu bytes\n", m, n,
             nb, kNoallocBytes);
     return QRDM_ERR_UNSUPPORTED;

@@ -99,7 +99,7 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
     const int buf = i & 1;
     double* part = p.part + (size_t)buf * G * stride;
     const double* rowb = p.rowbuf + (size_t)buf * (QRDM_NB_MAX + 2);
-    if (!grid_barrier(p.bar, (unsigned)G * (unsigned)(i + 1), &p.st->err)) {
+    if (!grid_barrier(p.bar, (unsigned)G * (unsigned)(i + 1), &p.st->err, p.spin_limit)) {
       ok = false;
       break;
     }
@@ -402,7 +402,7 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
       const unsigned target = (unsigned)G * (unsigned)(i + 1);
       unsigned spins = 0;
       while (ld_acquire_u32(p.bar) < target) {
-        if (++spins > QRDM_SPIN_LIMIT || (*(volatile int*)&p.st->err & QRDM_EDEV_BARRIER_TIMEOUT)) {
+        if (++spins > p.spin_limit || (*(volatile int*)&p.st->err & QRDM_EDEV_BARRIER_TIMEOUT)) {
           atomicOr(&p.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
           sm.exit_flag = 2;
           break;

@@ -7,8 +7,8 @@ notebook), so these fixtures are the known answers that pin both the CPU
 oracle and the GPU library.  Inputs are stored with the outputs, so the
 fixtures do not depend on the generator's floating-point reproducibility.
 
-Run in the container that holds the reference sources:
-    OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py
+Run where the reference sources are present, naming their root:
+    QRDM_REFERENCE_ROOT=<reference root> OPENBLAS_NUM_THREADS=1 python tests/golden/make_golden.py
 """
 from __future__ import annotations
 

@@ -11,7 +11,8 @@ PCG64 streams are platform independent), and the fixture keeps the base
 index of every column plus a seeded sample of entries to check that the
 regenerated matrix is the one the reference saw.
 
-Run in the container that holds the reference sources:
+Run after the compiled reference exists (oracle/build_ref.sh, or
+__graft_entry__.build() where the reference sources are present):
     python tests/golden/make_selection_golden.py
 """
 from __future__ import annotations

@@ -1,4 +1,4 @@
-"""Mixed-precision DM-QR: the trailing update on BF16 tensor cores through an
+"""Mixed-precision DM-QR: the trailing update on FP16 tensor cores through an
 Ozaki split (FP64 emulation).  Same parity bar as the FP64 path: identical
 jpvt / DM blocks over the gap-separated prefix of the oracle's run, backward
 error <= 10 max(m,n) eps, orthogonality <= 100 max(m,n) eps."""
