@@ -179,6 +179,19 @@ int qrdm_dgeqrf_dev(int matrix_layout, int m, int n, double* d_a, int lda, doubl
 int qrdm_dormqr_dev(int matrix_layout, int m, int n, int k, const double* d_a, int lda,
                     const double* d_tau, double* d_c, int ldc);
 
+/* ------------------------------------------------- rank-revealing helpers */
+/* The device side of the reference's verification helpers (auxil.py:20-200,
+ * checkQR and low_rank), which form A P and Frobenius norms on the host.
+ * out(:, j) = a(:, jpvt[j] - 1) for j < n: the columns of the m x n device
+ * matrix a in the order of a 1-based jpvt (device), i.e. A P; out must not
+ * overlap a.  Returns -5 if an entry of jpvt is outside [1, n]. */
+int qrdm_apply_jpvt_dev(int m, int n, const double* d_a, int lda, const int* d_jpvt, double* d_out,
+                        int ldo);
+/* *norm = ||X - Y||_F of two m x n device matrices (Y = NULL: ||X||_F),
+ * reduced on the device in a fixed order. */
+int qrdm_norm_diff_dev(int m, int n, const double* d_x, int ldx, const double* d_y, int ldy,
+                       double* norm);
+
 /* ------------------------------------------------------------- runtime */
 /* Make subsequent calls run on this cudaStream_t (NULL, the default: the
  * legacy default stream, ordered with the caller's other blocking streams).

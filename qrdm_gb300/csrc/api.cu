@@ -1221,6 +1221,63 @@ int qrdm_panel_phase_cycles(unsigned long long* out, int nout) {
   return 0;
 }
 
+// ------------------------------------------------- rank-revealing helpers
+// The device side of auxil.checkQR / low_rank (auxil.py:20-200): the
+// pivoted matrix A P and Frobenius norms of differences, so that the checks
+// run where the factors are.
+int qrdm_apply_jpvt_dev(int m, int n, const double* d_a, int lda, const int* d_jpvt, double* d_out,
+                        int ldo) {
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (lda < std::max(1, m)) return -4;
+  if (ldo < std::max(1, m)) return -7;
+  if (m == 0 || n == 0) return 0;
+  if (!d_a || !d_jpvt || !d_out) return -3;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  std::vector<int> hj(n);
+  CK(cudaMemcpyAsync(hj.data(), d_jpvt, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (int j = 0; j < n; ++j)
+    if (hj[j] < 1 || hj[j] > n) return -5;  // not a 1-based column index
+  k_apply_jpvt<<<dim3(ceil_div(m, 1024), n), 256, 0, s>>>(m, d_a, lda, d_jpvt, d_out, ldo);
+  RET(check_launch());
+  CK(cudaStreamSynchronize(s));
+  return 0;
+}
+
+int qrdm_norm_diff_dev(int m, int n, const double* d_x, int ldx, const double* d_y, int ldy,
+                       double* norm) {
+  if (!norm) return -7;
+  *norm = 0.0;
+  if (m < 0) return -1;
+  if (n < 0) return -2;
+  if (ldx < std::max(1, m)) return -4;
+  if (d_y && ldy < std::max(1, m)) return -6;
+  if (m == 0 || n == 0) return 0;
+  if (!d_x) return -3;
+  std::lock_guard<std::mutex> lk(g_mu);
+  Ctx* c = nullptr;
+  int r = ctx_get(&c);
+  if (r) return r;
+  cudaStream_t s = c->stream();
+  const int np = std::max(1, std::min(n, 4 * c->nsm));
+  CK(c->u_part.ensure(sizeof(double) * (size_t)(np + 1)));
+  double* part = c->u_part.as<double>();
+  k_sumsq_part<<<np, 256, 0, s>>>(m, n, d_x, ldx, d_y, ldy, part);
+  RET(check_launch());
+  k_sumsq_final<<<1, 32, 0, s>>>(part, np, part + np);
+  RET(check_launch());
+  double h = 0.0;
+  CK(cudaMemcpyAsync(&h, part + np, sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  *norm = std::sqrt(h);
+  return 0;
+}
+
 int qrdm_set_stream(void* stream) {
   std::lock_guard<std::mutex> lk(g_mu);
   Ctx* c = nullptr;
@@ -1241,7 +1298,8 @@ int qrdm_release_workspace(void) {
   Buf* bufs[] = {&c.a, &c.jpvt, &c.tau, &c.nrm, &c.list, &c.cand_a, &c.cand_b, &c.cand, &c.gram_part,
                  &c.gram, &c.perm, &c.st, &c.pan_part, &c.pan_row, &c.pan_bar, &c.vtv_part, &c.vtv,
                  &c.T, &c.wpart, &c.w2, &c.qF, &c.qg, &c.qpart, &c.qst,
-                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws, &c.b_prof, &c.pan_prof};
+                 &c.oz_va2, &c.oz_vb1, &c.oz_wb2, &c.oz_wexp, &c.oz_wp, &c.b_meta, &c.b_ws, &c.b_prof, &c.pan_prof,
+                 &c.u_part};
   if (c.b_graph) {
     cudaGraphExecDestroy(c.b_graph);
     c.b_graph = nullptr;

@@ -54,6 +54,7 @@ struct Ctx {
   Buf oz_va2, oz_vb1, oz_wb2, oz_wexp, oz_wp;  // mixed-precision trailing update
   Buf b_meta, b_ws, b_prof;                     // batched DM-QR
   Buf pan_prof;                                 // panel phase cycles (timing runs)
+  Buf u_part;                                   // rank helpers: norm partials
   // panel: dynamic shared memory that keeps one CTA per SM (0: not set)
   size_t pan_smem_floor = 0;
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch

@@ -149,6 +149,13 @@ int batched_nmax();
 int batched_kmax();
 long long batched_ws_doubles(int nmax, int mixed);
 
+// util.cu (rank-revealing helpers)
+__global__ void k_apply_jpvt(int m, const double* A, long long lda, const int* jpvt, double* out,
+                             long long ldo);
+__global__ void k_sumsq_part(int m, int n, const double* X, long long ldx, const double* Y, long long ldy,
+                             double* part);
+__global__ void k_sumsq_final(const double* part, int np, double* out);
+
 // qp3.cu
 struct Qp3State;
 size_t qp3_state_bytes();
