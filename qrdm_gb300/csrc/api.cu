@@ -493,7 +493,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     PH(4);
     // ---- partial-norm downdate with recompute safeguard (norm_update)
     {
-      k_norm_downdate<<<ceil_div(nloc, 256), 256, 0, s>>>(P.A, lda, j, n, nrm, nrm_exact, c.list.as<int>(), d_st);
+      k_norm_downdate<<<ceil_div(nloc, 32), 128, 0, s>>>(P.A, lda, j, n, nrm, nrm_exact, c.list.as<int>(), d_st);
       RET(check_launch());
       int blocks = std::min(ceil_div(nloc, 8), 4 * nsm);
       k_norm_recompute<<<std::max(1, blocks), 256, 0, s>>>(P.A, lda, j, m, c.list.as<int>(), nrm, nrm_exact, d_st);

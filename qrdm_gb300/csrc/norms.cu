@@ -36,44 +36,62 @@ __global__ void k_colnorm_init(const double* __restrict__ A, long long lda, int 
 }
 
 // Downdate of the partial norms of columns c0..n-1 after the block of fjb_cmp
-// new R rows (rows j..j+fjb_cmp-1).  One thread per column, the squares
-// summed in row order with separately rounded multiply and add, as the
+// new R rows (rows j..j+fjb_cmp-1).  A CTA takes 32 columns: its warps
+// stage the columns' new R rows in shared memory (each warp reads 256
+// contiguous bytes of one column per load), then one thread per column sums
+// the squares in row order with separately rounded multiply and add, as the
 // reference's loop (src/dgeqrdm_work.c:84-86).  Columns whose estimate fails
 // the safeguard are appended to `list` for a from-scratch recompute.
-__global__ void k_norm_downdate(const double* __restrict__ A, long long lda, int j, int n,
-                                double* __restrict__ nrm, double* __restrict__ nrm_exact,
-                                int* __restrict__ list, BlockState* st) {
-  int fjb_cmp = st->fjb_cmp;
-  int c0 = j + fjb_cmp;
-  int c = c0 + blockIdx.x * blockDim.x + threadIdx.x;
+constexpr int kDowndateCols = 32;
+
+__global__ void __launch_bounds__(128) k_norm_downdate(const double* __restrict__ A, long long lda, int j, int n,
+                                                       double* __restrict__ nrm, double* __restrict__ nrm_exact,
+                                                       int* __restrict__ list, BlockState* st) {
+  __shared__ double sr[kDowndateCols][QRDM_NB_MAX + 1];
+  const int fjb_cmp = min(st->fjb_cmp, QRDM_NB_MAX);
+  const int cb = j + fjb_cmp + blockIdx.x * kDowndateCols;
+  if (cb >= n) return;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)blockDim.x >> 5;
+  for (int cc = wid; cc < kDowndateCols; cc += nw) {
+    const int c = cb + cc;
+    if (c >= n) break;
+    const double* col = A + (size_t)c * lda + j;
+    for (int i = lane; i < fjb_cmp; i += 32) sr[cc][i] = col[i];
+  }
+  __syncthreads();
   // the new maximum is reduced over the warp first: one atomic per warp
   // instead of one per column on the same address
   unsigned long long mx = 0ull;
-  if (c < n) {
-    double w = nrm[c];
-    if (w != 0.0) {
-      const double* col = A + (size_t)c * lda + j;
-      double s = 0.0;
+  if (threadIdx.x < kDowndateCols) {
+    const int c = cb + threadIdx.x;
+    if (c < n) {
+      double w = nrm[c];
+      if (w != 0.0) {
+        const double* row = sr[threadIdx.x];
+        double s = 0.0;
 #pragma unroll 8
-      for (int i = 0; i < fjb_cmp; ++i) s = mul_add_rn(col[i], col[i], s);
-      double t = sqrt(fabs(s)) / w;
-      double d2 = (t + 1.0) * (1.0 - t);
-      t = (0.0 >= d2) ? 0.0 : d2;
-      double r = w / nrm_exact[c];
-      double t2 = t * (r * r);
-      const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53)
-      if (t2 <= tol3z) {
-        int slot = atomicAdd(&st->recompute, 1);
-        list[slot] = c;
-      } else {
-        w *= sqrt(t);
-        nrm[c] = w;
-        if (w > 0.0) mx = (unsigned long long)__double_as_longlong(w);
+        for (int i = 0; i < fjb_cmp; ++i) s = mul_add_rn(row[i], row[i], s);
+        double t = sqrt(fabs(s)) / w;
+        double d2 = (t + 1.0) * (1.0 - t);
+        t = (0.0 >= d2) ? 0.0 : d2;
+        double r = w / nrm_exact[c];
+        double t2 = t * (r * r);
+        const double tol3z = 1.0536712127723509e-08;  // sqrt(2^-53)
+        if (t2 <= tol3z) {
+          int slot = atomicAdd(&st->recompute, 1);
+          list[slot] = c;
+        } else {
+          w *= sqrt(t);
+          nrm[c] = w;
+          if (w > 0.0) mx = (unsigned long long)__double_as_longlong(w);
+        }
       }
     }
   }
-  mx = warp_max_u64(mx);
-  if ((threadIdx.x & 31) == 0 && mx) atomicMax(&st->maxnrm_bits, mx);
+  if (wid == 0) {
+    mx = warp_max_u64(mx);
+    if (lane == 0 && mx) atomicMax(&st->maxnrm_bits, mx);
+  }
 }
 
 // From-scratch partial norms of the listed columns over the rows below the

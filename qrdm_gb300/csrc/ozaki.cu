@@ -233,7 +233,8 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 //
 // Warp-specialised pipeline per 64-row block.  Sixteen converter warps
 // turn C from FP64 into its digits (the A operand), half a block (32 rows =
-// K16 steps 2h, 2h+1) at a time, into one of two half-buffers, and announce
+// K16 steps 2h, 2h+1) at a time, four rows of a column per thread (one
+// 8-byte shared store per digit), into one of two half-buffers, and announce
 // each half on an mbarrier; the loads of the next half are in flight
 // meanwhile.  One more warp (one lane) waits for a half, issues its
 // digit-pair MMAs and commits them to that half's "free" barrier, and keeps
@@ -266,7 +267,6 @@ __device__ __forceinline__ int oz_g1_exp(const OzG1Args& g, int c, int fjb) {
 
 constexpr int OZ_G1_CONV = 16;                         // converter warps
 constexpr int OZ_G1_THREADS = 32 * (OZ_G1_CONV + 1);  // + 1 MMA warp
-constexpr int OZ_G1_PAIRS = 2048 / (32 * OZ_G1_CONV);  // row pairs per thread per half block
 constexpr int OZ_G1_CPT = 256 / OZ_G1_CONV;            // drained reflector columns per thread
 
 template <int S>
@@ -352,44 +352,49 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
       acc_hi[i] = 0;
       acc_mid[i] = 0.f;
     }
-    // C rows r0 + 32 h + [0, 32) x the tile's 128 columns: row pairs spread
-    // over the converter threads, 16 consecutive threads on one column (256
-    // contiguous bytes); column cc = (tid >> 4) + 32 u of the tile
-    double2 xv[OZ_G1_PAIRS];
+    // C rows rb + [0, 32) x the tile's 128 columns per half block: quads of
+    // rows (4 q .. 4 q + 3, q = lane & 7) of two columns per thread; the
+    // four columns of a warp are {0, 4, 1, 5} + 2 (w & 1) + 8 (w >> 1)
+    // (+ 64 for the second), so a warp's 8-byte digit stores cover both
+    // bank halves of the swizzled tile
+    const int q4 = lane & 7;
+    const int colq = (int)((0x5140u >> (4 * (lane >> 3))) & 15u) + 2 * (w & 1) + 8 * (w >> 1);
+    double2 xv[2][2];
     auto load_half = [&](int ib, int h) {
       const int it = it0 + (ib >> 2);
       const int c0 = (it / g.nchunk) * 128;
-      const int rb = (it % g.nchunk) * 256 + (ib & 3) * 64 + 32 * h;
+      const int r = (it % g.nchunk) * 256 + (ib & 3) * 64 + 32 * h + 4 * q4;
 #pragma unroll
-      for (int u = 0; u < OZ_G1_PAIRS; ++u) {
-        const int e = tid + 32 * OZ_G1_CONV * u;
-        const int rp = e & 15, cc = e >> 4;
-        const int c = c0 + cc, r = rb + 2 * rp;
-        double2 x = make_double2(0.0, 0.0);
+      for (int u = 0; u < 2; ++u) {
+        const int c = c0 + colq + 64 * u;
+        double x[4] = {0.0, 0.0, 0.0, 0.0};
         if (c < fjb) {
           // reflector column: V (unit diagonal, zeros above); selected but
           // unfactored columns: zero
           if (c < k) {
             const double* col = g.W0 + (size_t)c * g.lda;
-            x.x = r > c && r < g.mloc ? __ldg(col + r) : (r == c ? 1.0 : 0.0);
-            x.y = r + 1 > c && r + 1 < g.mloc ? __ldg(col + r + 1) : (r + 1 == c ? 1.0 : 0.0);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              x[i] = r + i > c && r + i < g.mloc ? __ldg(col + r + i) : (r + i == c ? 1.0 : 0.0);
           }
         } else if (c < g.ncols) {
           const double* col = g.W0 + (size_t)c * g.lda;
-          if (r + 1 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
-            x = __ldg(reinterpret_cast<const double2*>(col + r));
+          if (r + 3 < g.mloc && ((((uintptr_t)(col + r)) & 15) == 0)) {
+            const double2 a = __ldg(reinterpret_cast<const double2*>(col + r));
+            const double2 b = __ldg(reinterpret_cast<const double2*>(col + r + 2));
+            x[0] = a.x; x[1] = a.y; x[2] = b.x; x[3] = b.y;
           } else {
-            if (r < g.mloc) x.x = __ldg(col + r);
-            if (r + 1 < g.mloc) x.y = __ldg(col + r + 1);
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+              if (r + i < g.mloc) x[i] = __ldg(col + r + i);
           }
         }
-        xv[u] = x;
+        xv[u][0] = make_double2(x[0], x[1]);
+        xv[u][1] = make_double2(x[2], x[3]);
       }
     };
-    // shifts of this thread's conversion columns for the current tile, two
-    // 16-bit fields per word (|shift| < 2^11; registers are the limit here)
     int cur_t = -1;
-    uint32_t shp[OZ_G1_PAIRS / 2];
+    int shc[2] = {0, 0};
     load_half(0, 0);
     for (int ib = 0; ib < nblk; ++ib) {
       const int kb = ib & 3;
@@ -398,28 +403,20 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
       if (t != cur_t) {
         cur_t = t;
 #pragma unroll
-        for (int u = 0; u < OZ_G1_PAIRS; u += 2) {
-          const int c = t * 128 + ((tid + 32 * OZ_G1_CONV * u) >> 4);
-          const int c2 = c + (32 * OZ_G1_CONV >> 4);
-          const int s0 = 8 * S - oz_g1_exp(g, c, fjb);
-          const int s1 = 8 * S - oz_g1_exp(g, c2, fjb);
-          shp[u / 2] = ((uint32_t)s0 & 0xFFFFu) | ((uint32_t)s1 << 16);
-        }
+        for (int u = 0; u < 2; ++u) shc[u] = 8 * S - oz_g1_exp(g, t * 128 + colq + 64 * u, fjb);
       }
 #pragma unroll
       for (int h = 0; h < 2; ++h) {
         // the MMAs that read this half for the previous block are complete
         if (ib >= 1 && !tc::mbar_wait(&aempty[h], (uint32_t)((ib - 1) & 1))) fail = true;
 #pragma unroll
-        for (int u = 0; u < OZ_G1_PAIRS; ++u) {
-          const int e = tid + 32 * OZ_G1_CONV * u;
-          const int rp = e & 15, cc = e >> 4;
-          const int sh = (u & 1) ? (int)shp[u / 2] >> 16 : (int)(short)(shp[u / 2] & 0xFFFFu);
-          uint32_t dp[S];
-          digits2_f16<S>(xv[u].x, xv[u].y, sh, dp);
-          const uint32_t off = tc::sw128_offset(cc, 32 * h + 2 * rp);
+        for (int u = 0; u < 2; ++u) {
+          uint32_t da[S], db[S];
+          digits2_f16<S>(xv[u][0].x, xv[u][0].y, shc[u], da);
+          digits2_f16<S>(xv[u][1].x, xv[u][1].y, shc[u], db);
+          const uint32_t off = tc::sw128_offset(colq + 64 * u, 32 * h + 4 * q4);
 #pragma unroll
-          for (int p = 0; p < S; ++p) *reinterpret_cast<uint32_t*>(adig + p * 16384 + off) = dp[p];
+          for (int p = 0; p < S; ++p) *reinterpret_cast<uint2*>(adig + p * 16384 + off) = make_uint2(da[p], db[p]);
         }
         tc::fence_async_smem();
         __syncwarp();

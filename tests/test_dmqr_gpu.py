@@ -74,6 +74,20 @@ def check_against(A0, gpu, ref, prefix, label: str):
     return met
 
 
+def agreement(gpu, ref):
+    """(blocks, columns) of the leading DM blocks in which the GPU run made
+    the same choices as the oracle's run: equal block sizes and equal pivots
+    over each block."""
+    rn, gn = ref["ncols"], gpu["ncols"]
+    nblk = int(np.count_nonzero(rn))
+    b = cols = 0
+    while b < nblk and gn[b] == rn[b] and np.array_equal(gpu["jpvt"][cols:cols + rn[b]],
+                                                          ref["jpvt"][cols:cols + rn[b]]):
+        cols += int(rn[b])
+        b += 1
+    return b, cols
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
 def test_golden_case(gpu_lib, golden, oracle, name):
@@ -88,29 +102,56 @@ def test_golden_case(gpu_lib, golden, oracle, name):
 
 
 @pytest.mark.gpu
-def test_config1_graded_1000(gpu_lib, oracle):
-    """DM-QR CPU-parity workload: 1000 x 1000, s_i = 10^(-12 (i-1)/999)."""
-    from oracle.oracle import run_dmqr
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_config1_graded_1000(gpu_lib, oracle, record_property, precision):
+    """DM-QR CPU-parity workload: 1000 x 1000, s_i = 10^(-12 (i-1)/999).
+    Pinned exactly over the oracle's gap-separated prefix (5 of its 17 DM
+    blocks, 301 columns: from block 6 on the margins fall to 12.8 and less
+    noise units); how far the run agrees beyond it is measured and reported
+    (record_property "agree_blocks"/"agree_cols")."""
     from qrdm_gb300 import workloads as W
 
     A0 = W.graded_svd(1000, seed=0)
     prefix, ref = separated(oracle, A0, (0.9, 0.15, 64, 0, 0.0))
     assert prefix[0] >= 5, prefix
-    gpu = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
-    check_against(A0, gpu, ref, prefix, label="config1")
+    gpu = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0), precision=precision)
+    check_against(A0, gpu, ref, prefix, label=f"config1-{precision}")
+    blocks, cols = agreement(gpu, ref)
+    record_property("prefix_blocks", prefix[0])
+    record_property("agree_blocks", blocks)
+    record_property("agree_cols", cols)
+    print(f"config1 {precision}: separated prefix {prefix[0]} blocks / {prefix[1]} columns; "
+          f"identical choices over {blocks} of {int(np.count_nonzero(ref['ncols']))} blocks, "
+          f"{cols} of 1000 columns")
+    assert blocks >= prefix[0] and cols >= prefix[1], (blocks, cols, prefix)
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("kind", ["gaussian", "kahan"])
-def test_config2_4096(gpu_lib, oracle, kind):
+def test_config2_4096(gpu_lib, oracle, record_property, kind):
     """Plain FP64 DM-QR on 4096 x 4096: i.i.d. N(0,1) and the perturbed Kahan
-    matrix (pivot ties, norm downdating)."""
+    matrix (pivot ties, norm downdating).  The Gaussian run is pinned over
+    all of its 65 DM blocks.  Every column of the Kahan matrix has norm 1
+    (c^2 + s^2 = 1), so every order decision of the reference is a tie broken
+    by the 1e-14 perturbation and the rounding of the downdated norms: pivot
+    parity is undefined at that noise level (the separated prefix is empty),
+    and the test holds that run to the backward-error and orthogonality
+    bounds, reporting how far the choices agree anyway."""
     from qrdm_gb300 import workloads as W
 
     A0 = W.gaussian(4096, 4096, seed=1) if kind == "gaussian" else W.kahan(4096, seed=2)
     prefix, ref = separated(oracle, A0, (0.9, 0.15, 64, 0, 0.0))
     gpu = run_gpu(A0, (0.9, 0.15, 64, 0, 0.0))
     check_against(A0, gpu, ref, prefix, label=f"config2-{kind}")
+    blocks, cols = agreement(gpu, ref)
+    record_property("prefix_blocks", prefix[0])
+    record_property("agree_blocks", blocks)
+    record_property("agree_cols", cols)
+    print(f"config2 {kind}: separated prefix {prefix[0]} blocks / {prefix[1]} columns; "
+          f"identical choices over {blocks} of {int(np.count_nonzero(ref['ncols']))} blocks, {cols} columns")
+    if kind == "gaussian":
+        assert prefix[0] == int(np.count_nonzero(ref["ncols"])), prefix
+    assert blocks >= prefix[0], (blocks, prefix)
 
 
 @pytest.mark.gpu
