@@ -959,12 +959,29 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
       const double sci = S.sc[i];
       const double* x = W0 + (size_t)i * lda;
       const int nslot = fjb - i;
+      // the scaled column i below the diagonal, read by every warp for each
+      // of its slots, is staged once in shared memory (the stage area is
+      // free during the panel); the products are the same as computed in
+      // place, so the sums are unchanged
+      const bool staged = mloc - i - 1 <= kStage;
+      double* xsh = S.stage;  // row r of the column at xsh[r - i - 1]
+      if (staged) {
+        for (int r = i + 1 + tid; r < mloc; r += blockDim.x) xsh[r - i - 1] = x[r] * sci;
+        __syncthreads();
+      }
       for (int sl = wid; sl < nslot; sl += nw) {
         const double* y = W0 + (size_t)(i + sl) * lda;
         double acc = 0.0;
-        for (int r = i + 1 + lane; r < mloc; r += 32) {
-          const double xs = x[r] * sci;
-          acc = fma(xs, sl == 0 ? xs : y[r], acc);
+        if (staged) {
+          for (int r = i + 1 + lane; r < mloc; r += 32) {
+            const double xs = xsh[r - i - 1];
+            acc = fma(xs, sl == 0 ? xs : y[r], acc);
+          }
+        } else {
+          for (int r = i + 1 + lane; r < mloc; r += 32) {
+            const double xs = x[r] * sci;
+            acc = fma(xs, sl == 0 ? xs : y[r], acc);
+          }
         }
         acc = warp_sum(acc);
         if (lane == 0) S.red[sl] = acc;
