@@ -969,7 +969,39 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
         for (int r = i + 1 + tid; r < mloc; r += blockDim.x) xsh[r - i - 1] = x[r] * sci;
         __syncthreads();
       }
-      for (int sl = wid; sl < nslot; sl += nw) {
+      // four of a warp's slots at a time when staged: one shared load of x
+      // and four independent loads of the slot columns per row (each slot's
+      // sum keeps its own order, so the results do not change)
+      int sl_first = wid;
+      if (staged) {
+        for (; sl_first + 3 * nw < nslot; sl_first += 4 * nw) {
+          const double* y1 = W0 + (size_t)(i + sl_first + nw) * lda;
+          const double* y2 = W0 + (size_t)(i + sl_first + 2 * nw) * lda;
+          const double* y3 = W0 + (size_t)(i + sl_first + 3 * nw) * lda;
+          const double* y0 = W0 + (size_t)(i + sl_first) * lda;
+          const bool self = sl_first == 0;
+          double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+          for (int r = i + 1 + lane; r < mloc; r += 32) {
+            const double xs = xsh[r - i - 1];
+            const double v0 = self ? xs : y0[r], v1 = y1[r], v2 = y2[r], v3 = y3[r];
+            a0 = fma(xs, v0, a0);
+            a1 = fma(xs, v1, a1);
+            a2 = fma(xs, v2, a2);
+            a3 = fma(xs, v3, a3);
+          }
+          a0 = warp_sum(a0);
+          a1 = warp_sum(a1);
+          a2 = warp_sum(a2);
+          a3 = warp_sum(a3);
+          if (lane == 0) {
+            S.red[sl_first] = a0;
+            S.red[sl_first + nw] = a1;
+            S.red[sl_first + 2 * nw] = a2;
+            S.red[sl_first + 3 * nw] = a3;
+          }
+        }
+      }
+      for (int sl = sl_first; sl < nslot; sl += nw) {
         const double* y = W0 + (size_t)(i + sl) * lda;
         double acc = 0.0;
         if (staged) {
