@@ -38,7 +38,7 @@ def _stale(obj: str, deps) -> bool:
 def build(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(OBJ, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
-    headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + [
+    headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh")) + glob.glob(os.path.join(CSRC, "*.h"))) + [
         os.path.join(os.path.dirname(HERE), "include", "qrdm_gb300.h")]
     cc = nvcc()
     jobs = []

@@ -45,6 +45,8 @@ static int ctx_get(Ctx** out) {
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     c.smem_optin = (size_t)optin;
     CK(cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking));
+    CK(cudaStreamCreateWithFlags(&c.cpy, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&c.ev_cpy, cudaEventDisableTiming));
     CK(cudaHostAlloc((void**)&c.h_st, sizeof(BlockState), cudaHostAllocDefault));
     CK(cudaEventCreate(&c.ev0));
     CK(cudaEventCreate(&c.ev1));
@@ -101,7 +103,23 @@ struct DmqrProblem {
   double gram_margin = 0.0078125;  // mixed Gram: FP64 recheck band around delta
   int nfxd = 0;    // fixed leading columns already factored
   unsigned spin_limit = QRDM_SPIN_LIMIT;  // polls before a device-wide wait gives up
+  HostMirror* mirror = nullptr;  // host copy of the finished columns (host entry points)
 };
+
+// Send columns [mirror->done, upto) of A to the host copy on the copy
+// stream, once the kernels issued so far on s have finished.
+static int mirror_columns(Ctx& c, cudaStream_t s, const DmqrProblem& P, int upto) {
+  HostMirror* hm = P.mirror;
+  if (!hm || upto <= hm->done) return 0;
+  CK(cudaEventRecord(hm->ev, s));
+  CK(cudaStreamWaitEvent(hm->cs, hm->ev, 0));
+  const int nc = upto - hm->done;
+  CK(cudaMemcpy2DAsync(hm->a + (size_t)hm->done * hm->lda, sizeof(double) * (size_t)hm->lda,
+                       P.A + (size_t)hm->done * P.lda, sizeof(double) * (size_t)P.lda,
+                       sizeof(double) * (size_t)P.m, nc, cudaMemcpyDeviceToHost, hm->cs));
+  hm->done = upto;
+  return 0;
+}
 
 #define RET(x)                 \
   do {                         \
@@ -427,7 +445,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     {
       int msw = 2 * kmax + 2;
       size_t smem = sizeof(double) * 2 * msw + sizeof(int) * (2 * msw + 2 * kmax + 2 * msw) +
-                    sizeof(unsigned) * ((size_t)ceil_div(nloc, 32) + 4) + sizeof(double) * (size_t)kmax * kmax +
+                    sizeof(unsigned) * ((size_t)ceil_div(nloc, 32) + 4) + sizeof(double) * (size_t)kmax * (kmax + 1) +
                     sizeof(unsigned long long) * 2 * (size_t)kmax + 64;
       if (smem + 1024 > c.smem_optin) return QRDM_ERR_UNSUPPORTED;
       k_dm_pick<<<1, 256, smem, s>>>(c.cand.as<Cand>(), c.gram.as<double>(), km, nloc, kmax, P.delta,
@@ -519,6 +537,9 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     rechecks += hs.rechecks;
     maxnrm = bits_to_double(hs.maxnrm_bits);
     j += fjb_cmp;
+    // columns left of j are final: copy them back behind the next blocks
+    // (in chunks of at least 256 columns, or the rest of the run)
+    if (P.mirror && (j - P.mirror->done >= 256 || j >= minmn)) RET(mirror_columns(c, s, P, j));
     if (P.stop_mode >= 1 && P.stop_mode <= 3) {
       if (maxnrm * std::sqrt((double)(nloc - fjb_cmp)) <= eta) break;
     }
@@ -564,7 +585,8 @@ static int validate(int layout, int m, int n, int lda, const double* thres, int 
 
 int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, int* d_jpvt,
                        double* d_tau, int* ncols, const double* thres, int nb,
-                       const qrdm_options* opt, qrdm_stats* stats, int* hj_buf) {
+                       const qrdm_options* opt, qrdm_stats* stats, int* hj_buf,
+                       HostMirror* mirror) {
   int v = validate(layout, m, n, lda, thres, nb);
   if (v) return v;
   if (nb > QRDM_NB_MAX) return QRDM_ERR_UNSUPPORTED;
@@ -612,6 +634,7 @@ int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, i
   if (err) return err;
   CK(cudaMemcpyAsync(d_jpvt, hj, sizeof(int) * n, cudaMemcpyHostToDevice, s));
   CK(cudaStreamSynchronize(s));
+  P.mirror = mirror;
   int r = dmqr_run(c, P, stats);
   if (stats) stats->launches = g_launches;
   return r;
@@ -875,15 +898,33 @@ int dgeqrdm_ex(int matrix_layout, int m, int n, double* a, int lda, int* jpvt, d
   CK(c->jpvt.ensure(sizeof(int) * (size_t)n));
   CK(c->tau.ensure(sizeof(double) * (size_t)minmn));
   double* d_a = c->a.as<double>();
-  CK(cudaMemcpy2DAsync(d_a, sizeof(double) * m, a, sizeof(double) * (size_t)lda, sizeof(double) * m, n,
-                       cudaMemcpyHostToDevice, s));
+  if (lda == m)
+    CK(cudaMemcpyAsync(d_a, a, sizeof(double) * (size_t)m * n, cudaMemcpyHostToDevice, s));
+  else
+    CK(cudaMemcpy2DAsync(d_a, sizeof(double) * m, a, sizeof(double) * (size_t)lda, sizeof(double) * m, n,
+                         cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->jpvt.p, jpvt, sizeof(int) * n, cudaMemcpyHostToDevice, s));
   CK(cudaMemcpyAsync(c->tau.p, tau, sizeof(double) * minmn, cudaMemcpyHostToDevice, s));
+  // a page-locked host matrix receives its finished columns while later
+  // blocks run (a pageable one is written once, at the end: copies into
+  // pageable memory would stall the host between blocks)
+  cudaPointerAttributes pa{};
+  const bool pinned = cudaPointerGetAttributes(&pa, a) == cudaSuccess && pa.type == cudaMemoryTypeHost;
+  cudaGetLastError();
+  HostMirror hm{a, lda, 0, c->cpy, c->ev_cpy};
   r = dgeqrdm_dev_locked(*c, matrix_layout, m, n, d_a, m, c->jpvt.as<int>(), c->tau.as<double>(), ncols,
-                         thres, nb, opt, stats, nullptr);
-  if (r > 0 || r == -1) return r;  // device failure or invalid argument: outputs untouched
-  CK(cudaMemcpy2DAsync(a, sizeof(double) * (size_t)lda, d_a, sizeof(double) * m, sizeof(double) * m, n,
-                       cudaMemcpyDeviceToHost, s));
+                         thres, nb, opt, stats, nullptr, pinned ? &hm : nullptr);
+  if (pinned) CK(cudaStreamSynchronize(c->cpy));  // no copy outlives the call
+  if (r > 0 || r == -1) return r;  // device failure or invalid argument: the factor is not returned
+  const int from = pinned ? hm.done : 0;
+  if (from < n) {
+    if (lda == m)
+      CK(cudaMemcpyAsync(a + (size_t)from * m, d_a + (size_t)from * m, sizeof(double) * (size_t)m * (n - from),
+                         cudaMemcpyDeviceToHost, s));
+    else
+      CK(cudaMemcpy2DAsync(a + (size_t)from * lda, sizeof(double) * (size_t)lda, d_a + (size_t)from * m,
+                           sizeof(double) * m, sizeof(double) * m, n - from, cudaMemcpyDeviceToHost, s));
+  }
   CK(cudaMemcpyAsync(jpvt, c->jpvt.p, sizeof(int) * n, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(tau, c->tau.p, sizeof(double) * minmn, cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));

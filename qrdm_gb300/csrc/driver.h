@@ -62,6 +62,8 @@ struct Ctx {
   int b_err_off = 0;                            // int offset of its error word in b_meta
   unsigned long long b_key = 0;
   BlockState* h_st = nullptr;              // pinned host copy of the block record
+  cudaStream_t cpy = nullptr;              // device-to-host copies of finished columns
+  cudaEvent_t ev_cpy = nullptr;            // a finished block, for the copy stream
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   cudaEvent_t ph[8] = {};
   // the caller's stream (qrdm_set_stream); NULL = the legacy default stream,
@@ -71,11 +73,26 @@ struct Ctx {
 };
 
 
+// Host copy of the factor kept up to date while a factorisation runs: the
+// columns left of the current DM block never change again, so after each
+// block the newly finished ones are copied back on the copy stream, behind
+// the remaining blocks' kernels.  `done` counts the columns already sent.
+struct HostMirror {
+  double* a;         // page-locked host matrix, column-major
+  long long lda;     // its leading dimension
+  int done;
+  cudaStream_t cs;
+  cudaEvent_t ev;
+};
+
 // DM-QR on device-resident data with the workspace of c.  hj: host scratch
-// of n ints (jpvt staging).  Caller holds the library lock.
+// of n ints (jpvt staging); mirror: optional host copy kept up to date
+// (columns only; the caller copies the rest).  Caller holds the library
+// lock.
 int dgeqrdm_dev_locked(Ctx& c, int layout, int m, int n, double* d_a, int lda, int* d_jpvt,
                        double* d_tau, int* ncols, const double* thres, int nb,
-                       const qrdm_options* opt, qrdm_stats* stats, int* hj);
+                       const qrdm_options* opt, qrdm_stats* stats, int* hj,
+                       HostMirror* mirror = nullptr);
 
 // Bytes of each workspace buffer DM-QR needs for an m x n problem with block
 // nb on a device with nsm SMs (used to carve a fixed scratch area).

@@ -483,7 +483,10 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   unsigned* bits = reinterpret_cast<unsigned*>(s_swb + maxsw);
   __shared__ int s_nsel, s_nswap;
   int nwords = (ncols + 31) >> 5;
-  double* s_g = reinterpret_cast<double*>(bits + ((nwords + 3) & ~3));  // [nc][nc] cosines
+  // [nc][nc + 1] cosines: the odd row stride spreads a warp's column reads
+  // (fixed column, consecutive rows) over the banks
+  double* s_g = reinterpret_cast<double*>(bits + ((nwords + 3) & ~3));
+  const int lg = nc + 1;
   const int nc = st->nc;
   for (int w = threadIdx.x; w < nwords; w += blockDim.x) bits[w] = 0u;
   for (int base = 0; base < nc * nc; base += 8 * (int)blockDim.x) {  // 8 loads in flight per thread
@@ -496,7 +499,7 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int e = base + u * (int)blockDim.x + threadIdx.x;
-      if (e < nc * nc) s_g[e] = v[u];
+      if (e < nc * nc) s_g[(size_t)(e / nc) * lg + (e % nc)] = v[u];
     }
   }
   __syncthreads();
@@ -506,7 +509,7 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   // j < i and NOT |cos(j, i)| < delta, compared as bit patterns on the
   // integer pipes); then one thread runs the scan with 128-bit ANDs.
   {
-    unsigned long long* s_mask = reinterpret_cast<unsigned long long*>(s_g + (size_t)nc * nc);  // [nc][2]
+    unsigned long long* s_mask = reinterpret_cast<unsigned long long*>(s_g + (size_t)nc * lg);  // [nc][2]
     const unsigned long long delta_bits = abs_bits(delta);
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (int)blockDim.x >> 5;
     for (int i = wid; i < nc; i += nw) {
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const int j = 32 * q + lane;
-        const bool conflict = j < i && !(abs_bits(s_g[(size_t)j * nc + i]) < delta_bits);
+        const bool conflict = j < i && !(abs_bits(s_g[(size_t)j * lg + i]) < delta_bits);
         words[q] = __ballot_sync(0xffffffffu, conflict);
       }
       if (lane == 0) {
