@@ -486,8 +486,8 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
   // [nc][nc + 1] cosines: the odd row stride spreads a warp's column reads
   // (fixed column, consecutive rows) over the banks
   double* s_g = reinterpret_cast<double*>(bits + ((nwords + 3) & ~3));
-  const int lg = nc + 1;
   const int nc = st->nc;
+  const int lg = nc + 1;
   for (int w = threadIdx.x; w < nwords; w += blockDim.x) bits[w] = 0u;
   for (int base = 0; base < nc * nc; base += 8 * (int)blockDim.x) {  // 8 loads in flight per thread
     double v[8];
