@@ -607,7 +607,7 @@ struct OzG2Args {
 constexpr int OZ_G2_EPI = 16;                          // epilogue warps
 constexpr int OZ_G2_THREADS = 32 * (OZ_G2_EPI + 1);   // + 1 producer warp
 constexpr int OZ_G2_CPW = 32 / (OZ_G2_EPI / 4);        // tile columns per epilogue warp
-constexpr int NST2 = 3;              // W2 digit stages
+constexpr int NST2 = 2;  // W2 digit stages (a third one measured slower: its shared memory is taken from L1)
 
 template <int S>
 __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
