@@ -237,12 +237,14 @@ __device__ __forceinline__ void oz_levels8(uint32_t taddr_lane, int col0, long l
 // 8-byte shared store per digit), into one of two half-buffers, and announce
 // each half on an mbarrier; the loads of the next half are in flight
 // meanwhile.  One more warp (one lane) waits for a half, issues its
-// digit-pair MMAs and commits them to that half's "free" barrier, and keeps
-// the V digits (B operand) of the next block arriving by bulk copy into the
-// second of two buffers.  After the last block of a 256-row chunk the
-// converter warps drain the levels into their integer accumulators (16
-// reflector columns each) and release the TMEM to the next chunk; after the
-// last chunk of a column tile they write the tile's partial.
+// digit-pair MMAs and commits them to that half's "free" barrier, and brings
+// the V digits (B operand) of the next block by bulk copy into their one
+// buffer as soon as the block's MMAs have finished (a second buffer measured
+// slower: its 56 KB come out of L1, where the converters' spills live).
+// After the last block of a 256-row chunk the converter warps drain the
+// levels into their integer accumulators (16 reflector columns each) and
+// release the TMEM to the next chunk; after the last chunk of a column tile
+// they write the tile's partial.
 struct OzG1Args {
   const double* W0;     // window origin A(j, j)
   long long lda;
@@ -274,7 +276,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* adig = base;               // S x 16 KB: 128 C columns x 64 rows
-  unsigned char* bdig = base + S * 16384;   // 2 x S x 8 KB: 64 reflectors x 64 rows
+  unsigned char* bdig = base + S * 16384;   // S x 8 KB: 64 reflectors x 64 rows
   constexpr uint32_t BBYTES = S * 8192;
   __shared__ uint64_t afull[2], aempty[2], bfull[2], dready, dfree;
   __shared__ uint32_t s_tmem;
@@ -315,7 +317,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
       tc::bulk_g2s(bdig, vsrc(0), BBYTES, &bfull[0]);
       for (int ib = 0; ib < nblk; ++ib) {
         const int kb = ib & 3;
-        const uint32_t bsm = tc::smem_u32(bdig + (ib & 1) * BBYTES);
+        const uint32_t bsm = tc::smem_u32(bdig);
         for (int h = 0; h < 2; ++h) {
           if (!tc::mbar_wait(&afull[h], (uint32_t)(ib & 1))) fail = true;
           if (h == 0) {
@@ -323,18 +325,18 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
             // a chunk's first MMAs overwrite the levels: the previous
             // chunk must have been drained
             if (kb == 0 && ib > 0 && !tc::mbar_wait(&dfree, (uint32_t)(((ib >> 2) - 1) & 1))) fail = true;
-          } else if (ib + 1 < nblk) {
-            // every MMA of block ib-1 is complete (its last commit), so the
-            // other B buffer can take block ib+1
-            if (ib >= 1 && !tc::mbar_wait(&aempty[1], (uint32_t)((ib - 1) & 1))) fail = true;
-            const int nb = (ib + 1) & 1;
-            tc::mbar_arrive_expect_tx(&bfull[nb], BBYTES);
-            tc::bulk_g2s(bdig + nb * BBYTES, vsrc(ib + 1), BBYTES, &bfull[nb]);
           }
           tc::fence_after_sync();
           if (!fail) oz_issue<S>(tmem, tc::smem_u32(adig), 16384u, bsm, 2 * h, 2 * h + 2, kb == 0 && h == 0);
           tc::mma_commit(&aempty[h]);
           if (h == 1 && kb == 3) tc::mma_commit(&dready);
+          if (h == 1 && ib + 1 < nblk) {
+            // one B buffer: block ib+1's V digits once block ib's MMAs are done
+            if (!tc::mbar_wait(&aempty[1], (uint32_t)(ib & 1))) fail = true;
+            const int nb = (ib + 1) & 1;
+            tc::mbar_arrive_expect_tx(&bfull[nb], BBYTES);
+            tc::bulk_g2s(bdig, vsrc(ib + 1), BBYTES, &bfull[nb]);
+          }
         }
       }
       // the last commits have landed before the CTA releases TMEM
@@ -757,7 +759,7 @@ __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
 }
 
 // ------------------------------------------------------------ launchers
-static size_t oz_gemm1_smem(int s) { return (size_t)s * (16384 + 2 * 8192) + 1024; }
+static size_t oz_gemm1_smem(int s) { return (size_t)s * (16384 + 8192) + 1024; }
 static size_t oz_gemm2_smem(int s) { return (size_t)s * (16384 + NST2 * 4096) + 1024; }
 size_t oz_gemm_smem(int s) { return oz_gemm1_smem(s); }
 
