@@ -539,10 +539,11 @@ def run_ours(args):
         peaks, peak_kind = load_peaks()
         phase = {"select": sti.ms_select, "panel": sti.ms_panel, "tfactor": sti.ms_tfactor,
                  "trail": sti.ms_trail, "norm": sti.ms_norm}
-        pcy = (C.c_ulonglong * 8)()
-        L.qrdm_panel_phase_cycles(pcy, 8)
+        pcy = (C.c_ulonglong * 12)()
+        L.qrdm_panel_phase_cycles(pcy, 12)
         if pcy[7]:
-            pnames = ["block_sync", None, "grid_barrier", "totals", "scalars", "apply", "partials"]
+            pnames = ["block_sync", "derive_wait", "grid_barrier", "totals", "scalars_wait", "apply",
+                      "partials_wait", None, "scalars_own", "derive_own", "partials_own"]
             phase["panel_cta0_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames) if nm}
         nblk = int(sti.nblocks)
         if prec == 0:

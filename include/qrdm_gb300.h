@@ -144,9 +144,13 @@ int qrdm_batched_phase_cycles(unsigned long long* out, int nout);
 
 /* Panel phase cycles of CTA 0 summed over the panels of the last DM-QR call
  * made with stats.timing = 1: out[0..7] = block barrier before the grid
- * arrival, 0 (unused), grid barrier, reading the column totals, reflector
+ * arrival, corrections of a column group's later partials (grouped panel;
+ * 0 otherwise), grid barrier, reading the column totals, reflector
  * scalars, reflector application, next-column partials and their
- * additions, kernel lifetime.
+ * additions, kernel lifetime; out[8..10] (if nout > 8; grouped panel) =
+ * the parts of the scalars, corrections and partials phases that thread 0
+ * spent in its own work before the phase's block barrier (the rest of each
+ * is the wait at that barrier).
  * Instrumentation only (no counterpart in the reference). */
 int qrdm_panel_phase_cycles(unsigned long long* out, int nout);
 

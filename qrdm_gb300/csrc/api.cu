@@ -44,6 +44,11 @@ static int ctx_get(Ctx** out) {
     int optin = 0;
     CK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     c.smem_optin = (size_t)optin;
+    // panel columns per grid barrier: QRDM_PANEL_GROUP = 1, 2, 4 or 8
+    if (const char* e = getenv("QRDM_PANEL_GROUP")) {
+      const int v = atoi(e);
+      if (v == 1 || v == 2 || v == 4 || v == 8) c.pan_group = v;
+    }
     CK(cudaStreamCreateWithFlags(&c.own, cudaStreamNonBlocking));
     CK(cudaStreamCreateWithFlags(&c.cpy, cudaStreamNonBlocking));
     CK(cudaEventCreateWithFlags(&c.ev_cpy, cudaEventDisableTiming));
@@ -63,8 +68,7 @@ static int ctx_get(Ctx** out) {
 
 int set_kernel_attributes(int big) {
   {
-    CK(cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
-    CK(cudaFuncSetAttribute(k_panel_red, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192));
+    if (panel_set_attributes(big)) return QRDM_ERR_CUDA;
     CK(cudaFuncSetAttribute(k_topk_tile, cudaFuncAttributeMaxDynamicSharedMemorySize, kTopkTile * (int)sizeof(Cand)));
     CK(cudaFuncSetAttribute(k_dm_pick, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
     CK(cudaFuncSetAttribute(k_permute_columns, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 1024));
@@ -173,9 +177,9 @@ DmqrWorkspaceSizes dmqr_workspace_sizes(int m, int n, int nb, int nsm) {
   w.perm = sizeof(int2) * (size_t)(2 * (2 * kcap + 2));
   w.st = sizeof(BlockState);
   const int gmax = panel_ctas(m, nsm);
-  // k_panel partials [2][G][NB_MAX+1] or k_panel_red limb totals (3 NB_MAX (NB_MAX+1)/2)
-  w.pan_part = sizeof(double) * std::max<size_t>(2 * (size_t)gmax * (QRDM_NB_MAX + 1), 3 * (size_t)QRDM_NB_MAX * (QRDM_NB_MAX + 1) / 2);
-  w.pan_row = sizeof(double) * 2 * (QRDM_NB_MAX + 2);
+  // k_panel partials [2][G][NB_MAX+1] or the limb totals of k_panel_red / k_panel_grp
+  w.pan_part = sizeof(double) * std::max<size_t>(std::max<size_t>(2 * (size_t)gmax * (QRDM_NB_MAX + 1), panel_red_totals(QRDM_NB_MAX)), panel_grp_totals(QRDM_NB_MAX, kPanelGroupMax));
+  w.pan_row = sizeof(double) * 2 * kPanelGroupMax * (QRDM_NB_MAX + 2);
   w.pan_bar = sizeof(unsigned) * 4;
   w.vtv_part = sizeof(double) * (size_t)gmax * QRDM_NB_MAX * QRDM_NB_MAX;
   w.vtv = sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX;
@@ -279,13 +283,20 @@ static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t 
     const int G = panel_ctas(mloc, c.nsm), R = ceil_div(mloc, G);
     const size_t need = (size_t)(R | 1) * kmax * sizeof(double);  // odd slab stride
     const size_t smem = std::max(need, c.pan_smem_floor);
-    if (need + 8192 <= c.smem_optin && panel_red_per_sm(smem) >= 1) {
+    // columns per grid barrier: the configured group if its shared memory
+    // fits, else one
+    int group = c.pan_group;
+    if (group > 1 && !(need + panel_static_smem(group) + 1024 <= c.smem_optin && panel_red_per_sm(smem, group) >= 1))
+      group = 1;
+    if (need + panel_static_smem(1) + 1024 <= c.smem_optin && panel_red_per_sm(smem, group) >= 1) {
       pa.rows_per_cta = R;
-      // the limb totals of every panel column (3 per slot, kmax (kmax + 1) / 2
-      // slots at most) and the barrier counter start at zero
-      CK(cudaMemsetAsync(pa.part, 0, sizeof(unsigned long long) * 3 * (size_t)kmax * (kmax + 1) / 2, s));
+      // the limb totals (k_panel_red: every panel column's slots;
+      // k_panel_grp: its three group regions) and the barrier counter start
+      // at zero
+      const size_t ntot = group > 1 ? panel_grp_totals(kmax, group) : panel_red_totals(kmax);
+      CK(cudaMemsetAsync(pa.part, 0, sizeof(unsigned long long) * ntot, s));
       CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
-      if (launch_panel_red(pa, G, smem, s) == cudaSuccess) {
+      if (launch_panel_red(pa, G, smem, group, s) == cudaSuccess) {
         ++g_launches;
         *G_used = G;
         return 0;
@@ -336,8 +347,8 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
   CK(c.st.ensure(ws.st));
   CK(c.pan_part.ensure(ws.pan_part));
   if (timing) {
-    CK(c.pan_prof.ensure(sizeof(unsigned long long) * 8));
-    CK(cudaMemsetAsync(c.pan_prof.p, 0, sizeof(unsigned long long) * 8, s));
+    CK(c.pan_prof.ensure(sizeof(unsigned long long) * kPanelPhases));
+    CK(cudaMemsetAsync(c.pan_prof.p, 0, sizeof(unsigned long long) * kPanelPhases, s));
   }
   CK(c.pan_row.ensure(ws.pan_row));
   CK(c.pan_bar.ensure(ws.pan_bar));
@@ -652,8 +663,8 @@ static int dgeqrf_locked(Ctx& c, int m, int n, double* d_a, long long lda, doubl
   const int nbn = std::min(nbq, k);  // column norms of one panel
   CK(c.nrm.ensure(sizeof(double) * 2 * nbn));
   CK(c.st.ensure(sizeof(BlockState)));
-  CK(c.pan_part.ensure(sizeof(double) * std::max<size_t>(2 * (size_t)gmax * (QRDM_NB_MAX + 1), 3 * (size_t)QRDM_NB_MAX * (QRDM_NB_MAX + 1) / 2)));
-  CK(c.pan_row.ensure(sizeof(double) * 2 * (QRDM_NB_MAX + 2)));
+  CK(c.pan_part.ensure(sizeof(double) * std::max<size_t>(std::max<size_t>(2 * (size_t)gmax * (QRDM_NB_MAX + 1), panel_red_totals(QRDM_NB_MAX)), panel_grp_totals(QRDM_NB_MAX, kPanelGroupMax))));
+  CK(c.pan_row.ensure(sizeof(double) * 2 * kPanelGroupMax * (QRDM_NB_MAX + 2)));
   CK(c.pan_bar.ensure(sizeof(unsigned) * 4));
   CK(c.vtv_part.ensure(sizeof(double) * (size_t)gmax * QRDM_NB_MAX * QRDM_NB_MAX));
   CK(c.vtv.ensure(sizeof(double) * QRDM_NB_MAX * QRDM_NB_MAX));
@@ -1255,10 +1266,10 @@ int qrdm_panel_phase_cycles(unsigned long long* out, int nout) {
   if (r) return r;
   for (int k = 0; k < nout; ++k) out[k] = 0;
   if (!c->pan_prof.p) return 0;
-  unsigned long long h[8];
+  unsigned long long h[kPanelPhases];
   CK(cudaMemcpyAsync(h, c->pan_prof.p, sizeof h, cudaMemcpyDeviceToHost, c->stream()));
   CK(cudaStreamSynchronize(c->stream()));
-  for (int k = 0; k < nout && k < 8; ++k) out[k] = h[k];
+  for (int k = 0; k < nout && k < kPanelPhases; ++k) out[k] = h[k];
   return 0;
 }
 

@@ -57,6 +57,7 @@ struct Ctx {
   Buf u_part;                                   // rank helpers: norm partials
   // panel: dynamic shared memory that keeps one CTA per SM (0: not set)
   size_t pan_smem_floor = 0;
+  int pan_group = 4;  // DM panel columns per grid barrier (k_panel_grp), 1 = k_panel_red
   cudaGraphExec_t b_graph = nullptr;            // cached launch of the last batch
   int b_grid = 0;                               // CTAs of the last batched launch
   int b_err_off = 0;                            // int offset of its error word in b_meta

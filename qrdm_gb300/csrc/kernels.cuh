@@ -23,15 +23,15 @@ struct PanelArgs {  // every field is set by the launching code
   double* tau;        // tau + j
   const double* nrm;  // partial norms of the window columns (nrm + j)
   BlockState* st;     // reads fjb, writes fjb_cmp
-  double* part;       // k_panel: [2][G][NB_MAX+1] partials; k_panel_red: limb totals
-                      // (3 per slot, fjb (fjb + 1) / 2 slots), zero at launch
-  double* rowbuf;     // [2][NB_MAX+2]
+  double* part;       // k_panel: [2][G][NB_MAX+1] partials; k_panel_red / k_panel_grp:
+                      // limb totals (panel_red_totals / panel_grp_totals), zero at launch
+  double* rowbuf;     // [2][NB_MAX+2] (k_panel_grp<GS>: [2][GS][NB_MAX+2])
   unsigned* bar;      // grid-barrier counter, zero at launch
   double* vtv_part;   // [G][NB_MAX][NB_MAX]
   int rows_per_cta;
   int allow_exit;     // 1: DM early exit (dgeqr2_mia); 0: plain dgeqr2
   int skip_vtv;       // 1: leave the V^T V partials to the caller (mixed precision)
-  unsigned long long* prof;  // k_panel_red: CTA 0's per-phase cycles [8] (added to), or null
+  unsigned long long* prof;  // CTA 0's per-phase cycles [kPanelPhases] (added to), or null
   unsigned spin_limit;       // polls before a grid barrier gives up (QRDM_SPIN_LIMIT by default)
 };
 
@@ -93,8 +93,17 @@ __global__ void k_vtv_stored(const double* V, long long ldv, int mloc, int rows_
                              const BlockState* st, double* vtv_part);
 __global__ void k_panel(PanelArgs p);
 __global__ void k_panel_red(PanelArgs p);
-cudaError_t launch_panel_red(const PanelArgs& pa, int G, size_t smem, cudaStream_t s);
-int panel_red_per_sm(size_t smem);
+cudaError_t launch_panel_red(const PanelArgs& pa, int G, size_t smem, int group, cudaStream_t s);
+int panel_red_per_sm(size_t smem, int group);
+int panel_set_attributes(int smem_optin);
+size_t panel_static_smem(int group);
+constexpr int kPanelGroupMax = 8;  // largest column group of k_panel_grp
+constexpr int kPanelPhases = 12;   // panel phase-cycle counters (PanelArgs::prof)
+constexpr int kPanelLimbs = 5;     // integer limbs per exact panel total
+// limb totals k_panel_red uses for a panel of kmax columns (every column's
+// slots) and k_panel_grp (3 regions of GS x kmax slots), zero at launch
+inline size_t panel_red_totals(int kmax) { return (size_t)kPanelLimbs * kmax * (kmax + 1) / 2; }
+inline size_t panel_grp_totals(int kmax, int group) { return (size_t)3 * kPanelLimbs * group * kmax; }
 __global__ void k_vtv_reduce(const double* vtv_part, int G, const BlockState* st, double* vtv);
 __global__ void k_larft(const double* vtv, const double* tau, const BlockState* st, double* T,
                         int ldt);

@@ -220,15 +220,19 @@ __global__ void __launch_bounds__(256) k_panel(PanelArgs p) {
 }
 
 // Exact, order-independent sums of FP64 values across CTAs: a value is
-// written as three signed 64-bit limbs of 42 bits, L0 2^-122 + L1 2^-80 +
-// L2 2^-38 (the top limb unmasked, so |v| < 2^16), each added with red.add.
-// Every FP64 value in [2^-69, 2^16) is represented exactly (its 53 bits fall
-// inside the limbs); smaller ones lose what lies below 2^-122.  Integer
-// additions do not round, so the totals are the exact sums whatever the
-// order of arrival; up to 2^20 values per total keep every limb below 2^63.
+// written as five signed 64-bit limbs of 42 bits, L0 2^-194 + L1 2^-152 +
+// L2 2^-110 + L3 2^-68 + L4 2^-26 (|v| < 2^16), each nonzero part added
+// with red.add.  Every FP64 value in [2^-141, 2^16) is represented exactly
+// (its 53 bits fall inside the limbs); smaller ones lose what lies below
+// 2^-194.  The range reaches the squares of columns that have fallen to
+// rounding level inside a panel (entries near 2^-53 of the column's scale).
+// Integer additions do not round, so the totals are the exact sums whatever
+// the order of arrival; up to 2^20 values per total keep every limb below
+// 2^63.
 constexpr int kLimbBits = 42;
-constexpr int kLimbBase = 122;  // weight of limb 0: 2^-122
-constexpr int kLimbs = 3;
+constexpr int kLimbBase = 194;  // weight of limb 0: 2^-194
+constexpr int kLimbs = kPanelLimbs;
+static_assert(kLimbBits * (kLimbs - 1) - kLimbBase == -26, "top limb weight");
 
 __device__ __forceinline__ void limbs_add(double v, unsigned long long* acc) {
   const unsigned long long b = (unsigned long long)__double_as_longlong(v);
@@ -254,31 +258,48 @@ __device__ __forceinline__ void limbs_add(double v, unsigned long long* acc) {
   }
 }
 
-// The FP64 value of three limb totals: carries are propagated in integer
+// The FP64 value of a slot's limb totals: carries are propagated in integer
 // arithmetic (low limbs into [0, 2^42)), a negative total is negated limb
-// by limb and renormalised, and the three nonnegative limbs (each exact in
-// FP64) are summed, so the result is the exact total rounded (<= 2 ulp).
+// by limb and renormalised, and the two highest nonzero limbs are converted
+// and combined (the lower ones lie more than 84 bits below the top), so the
+// result is the exact total rounded (<= 2 ulp) with four FP64 instructions:
+// the limb weights are built with integer instructions.
 __device__ __forceinline__ double limbs_value(const unsigned long long* acc) {
-  long long t0 = (long long)__ldcg(acc), t1 = (long long)__ldcg(acc + 1), t2 = (long long)__ldcg(acc + 2);
-  long long c = t0 >> kLimbBits;
-  t0 -= c << kLimbBits;
-  t1 += c;
-  c = t1 >> kLimbBits;
-  t1 -= c << kLimbBits;
-  t2 += c;
-  const bool neg = t2 < 0;
-  if (neg) {
-    t0 = -t0;
-    t1 = -t1;
-    t2 = -t2;
-    c = t0 >> kLimbBits;
-    t0 -= c << kLimbBits;
-    t1 += c;
-    c = t1 >> kLimbBits;
-    t1 -= c << kLimbBits;
-    t2 += c;
+  long long t[kLimbs];
+#pragma unroll
+  for (int k = 0; k < kLimbs; ++k) t[k] = (long long)__ldcg(acc + k);
+#pragma unroll
+  for (int k = 0; k + 1 < kLimbs; ++k) {
+    const long long c = t[k] >> kLimbBits;
+    t[k] -= c << kLimbBits;
+    t[k + 1] += c;
   }
-  const double v = fma((double)t2, 0x1p-38, fma((double)t1, 0x1p-80, (double)t0 * 0x1p-122));
+  const bool neg = t[kLimbs - 1] < 0;
+  if (neg) {
+#pragma unroll
+    for (int k = 0; k < kLimbs; ++k) t[k] = -t[k];
+#pragma unroll
+    for (int k = 0; k + 1 < kLimbs; ++k) {
+      const long long c = t[k] >> kLimbBits;
+      t[k] -= c << kLimbBits;
+      t[k + 1] += c;
+    }
+  }
+  // highest nonzero limb h (h = 0 when all are zero) and the one below it
+  long long hi = t[0], lo = 0;
+  int h = 0;
+#pragma unroll
+  for (int k = 1; k < kLimbs; ++k) {
+    if (t[k] != 0) {
+      hi = t[k];
+      lo = t[k - 1];
+      h = k;
+    }
+  }
+  const int e_hi = kLimbBits * h - kLimbBase;  // weight of limb h: 2^e_hi (normal range)
+  const double w_hi = __longlong_as_double((long long)(1023 + e_hi) << 52);
+  const double w_lo = __longlong_as_double((long long)(1023 + e_hi - kLimbBits) << 52);
+  const double v = fma((double)hi, w_hi, (double)lo * w_lo);
   return neg ? -v : v;
 }
 
@@ -573,22 +594,572 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
   if (g == 0 && tid == 0) p.st->fjb_cmp = kc;
 }
 
-// Launch the integer-total panel (cooperative) on G CTAs; returns the CUDA
-// error of the launch.
-cudaError_t launch_panel_red(const PanelArgs& pa, int G, size_t smem, cudaStream_t s) {
-  void* args[] = {const_cast<PanelArgs*>(&pa)};
-  return cudaLaunchCooperativeKernel((void*)k_panel_red, dim3(G), dim3(256), args, smem, s);
+// ------------------------------------- grouped K-panel: GS columns / barrier
+// Same reflectors as k_panel_red (one CTA per SM, slabs in shared memory,
+// exact limb totals), with ONE grid barrier per group of GS panel columns
+// i .. i+GS-1 instead of one per column.  Before the barrier every CTA adds
+// the partials of all GS columns, each taken in the current state (after
+// H(0..i-1)): D_k(c) = sum_{r > i+k} A(r, i+k) A(r, c) over its rows, and the
+// CTAs holding rows i .. i+GS-1 publish them.  After it every CTA runs the
+// GS reflector steps on these sums alone: step j forms beta, tau and
+// tau w_c from D_j (already brought to the state of step j), then takes
+// H(i+j) = I - tau v v^T out of every later D_k:
+//   (y - t_y v).(z - t_z v) = y.z - t_z (y.v) - t_y (z.v) + t_y t_z (v.v)
+// summed over r > i+k, where v.z over r > i+k is scal (x.z - sum of the
+// group rows i+j+1 .. i+k of x and z), x = A(:, i+j) below its diagonal,
+// and the group rows are carried through the same updates.  Every CTA
+// does the same operations on the same totals, so all hold identical
+// scalars.  Then each CTA applies the accepted reflectors to its slab and,
+// in the same pass over the later columns, forms the next group's partials.
+// The partials of later columns thus come from the exact sums of the
+// earlier state plus rank-one corrections, whose rounding errors are a few
+// units of the column's size at the start of the group.  A reflector's
+// orthogonality depends on its column's squared norm relative to those
+// errors, so a group ends early (the next one starts with exact totals at
+// that column) when the earlier reflectors of the group have taken more than
+// 15/16 of the column's square; the corrected sums are then within ~16 x a
+// few units of the exact ones.
+//
+// Per step the scalar chain is short: one rsqrt gives |beta| = s rsqrt(s)
+// and 1/beta (s = alpha^2 + |x|^2), and the reciprocal 1/(alpha - beta)
+// runs beside it in a second warp (FP64 instructions with one active lane
+// occupy an SM sub-partition's FP64 pipe as long as a full warp's).
+template <int GS>
+struct PanelGrpSmem {
+  double sc[QRDM_NB_MAX], sc_inv[QRDM_NB_MAX];
+  double P[GS][QRDM_NB_MAX];       // P[k][c]: column i+k's partial with column c (c >= i+k)
+  double row[2][GS][QRDM_NB_MAX];  // rows i .. i+GS-1 of columns i .. fjb-1 (two states)
+  double tw[GS][QRDM_NB_MAX];      // tau_j w_c of the group's reflectors
+  double dy[GS], dv[GS];           // per step: x.(column i+k) and x.x over r > i+k, unscaled by scal
+  double P0[GS], R0[GS];           // column i+k's totals and diagonal entry before the corrections
+  double M[GS];                    // 1/16 of column i+k's square at the group's start
+  double scal[GS], beta[GS], tau[GS], rbeta[GS];
+  int tz[GS];
+  double thres;
+  int flag;  // 1: early exit, 2: barrier timeout, 3: group ends early
+};
+
+// Partials of group columns i .. i+s-1 over this CTA's rows, added into the
+// group's limb totals: slot (k, c), k < s, c in [i+k, fjb), at
+// tot[kLimbs (k fjb + c)]; four threads per slot as in panel_partials_red.
+// (Used for the first group; later groups' partials come from the fused
+// update pass.)
+__device__ __forceinline__ void panel_grp_partials(const double* __restrict__ S, int LS, int nr, int grow0,
+                                                   int i, int s, int fjb,
+                                                   unsigned long long* __restrict__ tot, int* err) {
+  const int w0 = fjb - i;                       // slots of column i
+  const int nsl = s * w0 - s * (s - 1) / 2;     // all slots of the group
+  const int part = threadIdx.x & 3;
+  for (int base = 0; base < nsl; base += (int)blockDim.x >> 2) {
+    const int q = base + ((int)threadIdx.x >> 2);
+    int k = 0, rem = q;
+    while (k < s && rem >= w0 - k) {
+      rem -= w0 - k;
+      ++k;
+    }
+    double a0 = 0.0, a1 = 0.0;
+    if (q < nsl) {
+      const double* x = S + (size_t)(i + k) * LS;
+      const double* y = S + (size_t)(i + k + rem) * LS;
+      int rr0 = i + k + 1 - grow0;
+      if (rr0 < 0) rr0 = 0;
+      int rr = rr0 + part;
+      for (; rr + 4 < nr; rr += 8) {
+        a0 = fma(x[rr], y[rr], a0);
+        a1 = fma(x[rr + 4], y[rr + 4], a1);
+      }
+      if (rr < nr) a0 = fma(x[rr], y[rr], a0);
+    }
+    double v = a0 + a1;
+    v += __shfl_xor_sync(0xffffffffu, v, 1);
+    v += __shfl_xor_sync(0xffffffffu, v, 2);
+    if (q < nsl && part == 0 && nr > 0) {
+      if ((abs_bits(v) >> 52) >= 1023ull + 16ull) atomicOr(err, QRDM_EDEV_PANEL_RANGE);
+      else limbs_add(v, tot + (size_t)kLimbs * (k * fjb + i + k + rem));
+    }
+  }
 }
 
-// CTAs of the integer-total panel that fit on one SM with this dynamic
-// shared memory (0 if it cannot run).
-int panel_red_per_sm(size_t smem) {
+// Publish rows i .. i+s-1 (those this CTA holds) of columns i .. fjb-1.
+__device__ __forceinline__ void panel_grp_rows(const double* __restrict__ S, int LS, int nr, int grow0, int i,
+                                               int s, int fjb, double* __restrict__ rb) {
+  for (int k = 0; k < s; ++k) {
+    const int r = i + k;
+    if (r < grow0 || r >= grow0 + nr) continue;
+    for (int c = i + (int)threadIdx.x; c < fjb; c += blockDim.x)
+      rb[(size_t)k * (QRDM_NB_MAX + 2) + c] = S[(size_t)c * LS + (r - grow0)];
+  }
+}
+
+// tau w_c of reflector j for column c (one expression, so that every use
+// of it rounds alike)
+__device__ __forceinline__ double grp_tw(double tau, double rb, double row_c, double p_c) {
+  return fma(tau, row_c, -rb * p_c);
+}
+
+template <int GS>
+__global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  double* S = reinterpret_cast<double*>(smem_raw);  // [fjb][LS]
+  __shared__ PanelGrpSmem<GS> sm;
+  const int G = gridDim.x, g = blockIdx.x, R = p.rows_per_cta;
+  const int LS = R | 1;
+  const int fjb = p.st->fjb;
+  const int grow0 = g * R;
+  const int nr = max(0, min(R, p.mloc - grow0));
+  const size_t lda = (size_t)p.lda;
+  double* W0 = p.A + (size_t)p.j * lda + p.j;
+  // limb totals: three regions of GS x fjb slots, used by groups in turn;
+  // group gi adds into region gi % 3 before barrier gi and reads it after,
+  // and region (gi + 2) % 3 (read by group gi-1 before barrier gi) is
+  // cleared during group gi, before barrier gi+1 orders the clearing ahead
+  // of group gi+2's additions.  (A group that ends early leaves its later
+  // columns to the next group, which sums them afresh.)
+  unsigned long long* acc = reinterpret_cast<unsigned long long*>(p.part);
+  const size_t region = (size_t)kLimbs * GS * fjb;
+  const int tid = threadIdx.x;
+  constexpr size_t kRowBuf = (size_t)GS * (QRDM_NB_MAX + 2);
+
+  for (int c = tid; c < fjb; c += blockDim.x) {
+    sm.sc[c] = pow2_scale_for(p.nrm[c]);
+    sm.sc_inv[c] = 1.0 / sm.sc[c];
+  }
+  if (tid == 0) {
+    sm.flag = 0;
+    sm.thres = 5e-14;
+  }
+  __syncthreads();
+  for (int e = tid; e < fjb * nr; e += blockDim.x) {
+    int c = e / nr, rr = e % nr;
+    S[(size_t)c * LS + rr] = W0[(size_t)c * lda + grow0 + rr] * sm.sc[c];
+  }
+  __syncthreads();
+  {
+    const int s0 = min(GS, fjb);
+    panel_grp_partials(S, LS, nr, grow0, 0, s0, fjb, acc, &p.st->err);  // region 0
+    panel_grp_rows(S, LS, nr, grow0, 0, s0, fjb, p.rowbuf);
+  }
+
+  int done = fjb;
+  bool ok = true;
+  const bool prof = p.prof != nullptr && g == 0 && tid == 0;
+  unsigned long long pc[kPanelPhases] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  long long tlast = clock64();
+  const long long tstart = tlast;
+#define PPH(k)                                       \
+  do {                                               \
+    if (prof) {                                      \
+      const long long now_ = clock64();              \
+      pc[(k)] += (unsigned long long)(now_ - tlast); \
+      tlast = now_;                                  \
+    }                                                \
+  } while (0)
+  int gi = 0;
+  for (int i = 0; i < fjb; ++gi) {
+    const int s = min(GS, fjb - i);
+    const double* rowb = p.rowbuf + (size_t)(gi & 1) * kRowBuf;
+    __syncthreads();
+    PPH(0);
+    if (tid == 0) {
+      sm.flag = 0;  // (a group that ended early set 3; every thread has read it)
+      red_release_add_u32(p.bar, 1u);
+      const unsigned target = (unsigned)G * (unsigned)(gi + 1);
+      unsigned spins = 0;
+      while (ld_acquire_u32(p.bar) < target) {
+        if (++spins > p.spin_limit || (*(volatile int*)&p.st->err & QRDM_EDEV_BARRIER_TIMEOUT)) {
+          atomicOr(&p.st->err, QRDM_EDEV_BARRIER_TIMEOUT);
+          sm.flag = 2;
+          break;
+        }
+        if (spins > 32) __nanosleep(20);
+      }
+    }
+    __syncthreads();
+    PPH(2);
+    if (sm.flag == 2) {
+      ok = false;
+      break;
+    }
+    // the group's totals and rows (rows past the window read as zero)
+    {
+      const int w0 = fjb - i;
+      const int nsl = s * w0 - s * (s - 1) / 2;
+      for (int q = tid; q < nsl; q += blockDim.x) {
+        int k = 0, rem = q;
+        while (k < s && rem >= w0 - k) {
+          rem -= w0 - k;
+          ++k;
+        }
+        const double t = limbs_value(acc + (size_t)(gi % 3) * region + (size_t)kLimbs * (k * fjb + i + k + rem));
+        sm.P[k][i + k + rem] = t;
+        if (rem == 0) sm.P0[k] = t;
+      }
+      {
+        unsigned long long* z = acc + (size_t)((gi + 2) % 3) * region;
+        for (size_t q = (size_t)g * blockDim.x + tid; q < region; q += (size_t)G * blockDim.x) z[q] = 0ull;
+      }
+      for (int q = tid; q < s * w0; q += blockDim.x) {
+        const int k = q / w0, c = i + q % w0;
+        const double t = (i + k < p.mloc) ? __ldcg(rowb + (size_t)k * (QRDM_NB_MAX + 2) + c) : 0.0;
+        sm.row[0][k][c] = t;
+        if (c == i + k) sm.R0[k] = t;
+      }
+    }
+    __syncthreads();
+    PPH(3);
+    int na = s;   // reflectors of the group that are accepted
+    int cur = 0;  // row buffer holding the current state
+    for (int j = 0; j < s; ++j) {
+      const int col = i + j;
+      double(*rw)[QRDM_NB_MAX] = sm.row[cur];
+      // A. scalars of column col: thread 0 the exit tests, beta, 1/beta and
+      //    tau; thread 32 the same beta and 1/(alpha - beta); warp 7 the
+      //    sums over the group rows that the corrections subtract
+      if (tid == 0 || tid == 32) {
+        // the chain is s -> rsqrt -> beta and tau = 1 + |alpha| / |beta|
+        // (thread 0); thread 32 forms 1/(alpha - beta) =
+        // sign(alpha) (|beta| - |alpha|) / |x|^2 with 1/|x|^2 taken beside
+        // the rsqrt when |x|^2 >= alpha^2 (then |beta| >= sqrt(2) |alpha|
+        // and the difference loses at most two bits), else as the
+        // reciprocal of alpha - beta; the tests resolve meanwhile
+        const double alpha = rw[j][col];
+        double red0 = sm.P[j][col];
+        red0 = red0 < 0.0 ? 0.0 : red0;  // a corrected square can round below zero
+        const double s2 = fma(alpha, alpha, red0);
+        const double r = rsqrt(s2);
+        const double aa = fabs(alpha);
+        int fl = 0, tz = 1;
+        if (j > 0 && s2 < sm.M[j]) {
+          // the group's earlier reflectors took more than 15/16 of this
+          // column's square: its corrected sums have lost too many bits,
+          // so the group ends here and the next one starts from exact
+          // totals at this column
+          fl = 3;
+        } else if (p.mloc - col > 1) {
+          const double t = sm.thres * sm.sc[col];
+          if (col > 0 && p.allow_exit && red0 < t * t) fl = 1;
+          else if (red0 != 0.0) tz = 0;
+        }
+        if (tid == 0) {
+          if (fl) {
+            sm.flag = fl;
+          } else {
+            const double mag = s2 * r;  // |beta|
+            const double beta = tz ? alpha : (alpha >= 0.0 ? -mag : mag);
+            const double rb = tz ? 0.0 : (alpha >= 0.0 ? -r : r);  // 1 / beta
+            const double tau = tz ? 0.0 : fma(aa, r, 1.0);          // (beta - alpha) / beta
+            if (col == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(beta) * sm.sc_inv[0];
+            sm.beta[j] = beta;
+            sm.tz[j] = tz;
+            sm.tau[j] = tau;
+            sm.rbeta[j] = rb;
+            if (g == 0) p.tau[col] = tau;
+          }
+        } else {
+          const double ir0 = __drcp_rn(red0);
+          if (!tz && !fl) {
+            const double mag = s2 * r;
+            double sc_ = red0 >= alpha * alpha ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
+            sm.scal[j] = alpha >= 0.0 ? sc_ : -sc_;
+          }
+        }
+      } else if (j == 0 && tid >= 192 && tid - 192 < s) {
+        const int k = tid - 192;
+        sm.M[k] = 0.0625 * fma(sm.R0[k], sm.R0[k], sm.P0[k]);
+      } else if (tid >= 224 && tid - 224 < s - 1 - j) {
+        const int k = j + 1 + (tid - 224);
+        double dy = sm.P[j][i + k], dv = sm.P[j][col];
+        for (int r = j + 1; r <= k; ++r) {
+          const double xr = rw[r][col];
+          dy = fma(-xr, rw[r][i + k], dy);
+          dv = fma(-xr, xr, dv);
+        }
+        sm.dy[k] = dy;
+        sm.dv[k] = dv;
+      }
+      PPH(8);
+      __syncthreads();
+      PPH(4);
+      if (sm.flag == 1 || sm.flag == 3) {
+        na = j;
+        break;
+      }
+      if (sm.tz[j]) continue;  // H(col) = I: nothing changes
+      // B. tau w_c of H(col); the later group columns' partials and rows
+      //    brought to the state after H(col) (rows into the other buffer)
+      {
+        const double tau = sm.tau[j], rb = sm.rbeta[j], scal = sm.scal[j];
+        double(*rn)[QRDM_NB_MAX] = sm.row[cur ^ 1];
+        const int w1 = fjb - col - 1;  // columns after col
+        const int nk = s - 1 - j;      // later group columns
+        const int npr = nk * w1 - nk * (nk - 1) / 2;
+        const int nrw = nk * w1;
+        const int ntot = npr + nrw + (nk == 0 ? w1 : 0);
+        for (int q = tid; q < ntot; q += blockDim.x) {
+          if (q < npr) {
+            int k = j + 1, rem = q;
+            while (rem >= fjb - i - k) {
+              rem -= fjb - i - k;
+              ++k;
+            }
+            const int c = i + k + rem;
+            const double twc = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
+            const double twk = grp_tw(tau, rb, rw[j][i + k], sm.P[j][i + k]);
+            double dz = sm.P[j][c];
+            for (int r = j + 1; r <= k; ++r) dz = fma(-rw[r][col], rw[r][c], dz);
+            const double Y = scal * sm.dy[k], V = (scal * scal) * sm.dv[k], Z = scal * dz;
+            double pn = sm.P[k][c];
+            pn = fma(-twc, Y, pn);
+            pn = fma(-twk, Z, pn);
+            pn = fma(twk * twc, V, pn);
+            sm.P[k][c] = pn;
+            if (k == j + 1) sm.tw[j][c] = twc;  // (k = j+1 covers every c > col once)
+          } else if (q < npr + nrw) {
+            const int e = q - npr, rk = j + 1 + e / w1, c = col + 1 + e % w1;
+            const double twc = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
+            const double v = rw[rk][col] * scal;  // the operations of the slab update
+            rn[rk][c] = fma(-v, twc, rw[rk][c]);
+          } else {
+            const int c = col + 1 + (q - npr - nrw);
+            sm.tw[j][c] = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
+          }
+        }
+      }
+      PPH(9);
+      __syncthreads();
+      PPH(1);
+      cur ^= 1;
+    }
+    // apply the na accepted reflectors to this CTA's rows, one thread per
+    // row: the group's own columns in order (each takes the earlier
+    // reflectors, then becomes v below its diagonal, beta on it), then the
+    // next group's columns (its x vectors); the later columns follow in one
+    // pass that also forms the next group's partials
+    unsigned live = 0;
+    for (int j = 0; j < na; ++j)
+      if (!sm.tz[j]) live |= 1u << j;
+    const int i2 = i + na;  // the next group's first column
+    const int s2 = (sm.flag == 1 || i2 >= fjb) ? 0 : min(GS, fjb - i2);
+    unsigned long long* tot2 = acc + (size_t)((gi + 1) % 3) * region;
+    if (live) {
+      for (int rr = tid; rr < nr; rr += blockDim.x) {
+        const int grow = grow0 + rr;
+        double vr[GS];  // v_j at this row (0 on and above its diagonal row)
+#pragma unroll
+        for (int k = 0; k < GS; ++k) {
+          vr[k] = 0.0;
+          if (k < na) {
+            double val = S[(size_t)(i + k) * LS + rr];
+#pragma unroll
+            for (int j = 0; j < k; ++j) {
+              if ((live >> j) & 1u) {
+                if (grow > i + j) val = fma(-vr[j], sm.tw[j][i + k], val);
+                else if (grow == i + j) val -= sm.tw[j][i + k];
+              }
+            }
+            if ((live >> k) & 1u) {
+              if (grow > i + k) {
+                val *= sm.scal[k];
+                vr[k] = val;
+              } else if (grow == i + k) {
+                val = sm.beta[k];
+              }
+            }
+            S[(size_t)(i + k) * LS + rr] = val;
+          }
+        }
+        for (int c = i2; c < i2 + s2; ++c) {
+          double val = S[(size_t)c * LS + rr];
+#pragma unroll
+          for (int j = 0; j < GS; ++j) {
+            if ((live >> j) & 1u) {
+              if (grow > i + j) val = fma(-vr[j], sm.tw[j][c], val);
+              else if (grow == i + j) val -= sm.tw[j][c];
+            }
+          }
+          S[(size_t)c * LS + rr] = val;
+        }
+      }
+      __syncthreads();
+    }
+    PPH(5);
+    // every column from i2 on: P threads per column (P a power of two from
+    // 4 to 32, as many as keep all warps busy; thread `part` takes the rows
+    // of one residue mod P, two rows per iteration), the update where it is
+    // still due, then the dot products with the next group's x vectors over
+    // the rows below each one's diagonal.  Row masks are folded into the
+    // coefficients: a reflector's entry is its v below its diagonal row, 1
+    // on it and 0 above (fma(-1, t, v) = v - t exactly), an x vector's 0 on
+    // and above its diagonal row.
+    if (fjb > i2 && (live || s2 > 0)) {
+      const int nc = fjb - i2;
+      int lgP = 2;
+      while (lgP < 5 && (nc << (lgP + 1)) <= (int)blockDim.x) ++lgP;
+      const int P = 1 << lgP, part = tid & (P - 1), cpp = (int)blockDim.x >> lgP;
+      // rows i2 .. i2+s2-1 that this CTA holds are published for the next
+      // group as they are finished (local rows pr0 .. pr0+s2-1)
+      const int pr0 = i2 - grow0;
+      const bool pub = s2 > 0 && pr0 < nr && pr0 + s2 > 0;
+      double* pubrow = p.rowbuf + (size_t)((gi + 1) & 1) * kRowBuf;
+      for (int base = 0; base < nc; base += cpp) {
+        const int cc = base + (tid >> lgP), c = i2 + cc;
+        double dacc[GS];
+#pragma unroll
+        for (int k = 0; k < GS; ++k) dacc[k] = 0.0;
+        if (cc < nc) {
+          const bool app = live && c >= i2 + s2;
+          double twv[GS];
+#pragma unroll
+          for (int j = 0; j < GS; ++j) twv[j] = ((live >> j) & 1u) ? sm.tw[j][c] : 0.0;
+          double* col_c = S + (size_t)c * LS;
+          for (int ra = part; ra < nr; ra += 2 * P) {
+            const int rb = ra + P;
+            const bool hb = rb < nr;
+            const int ga = grow0 + ra, gb = grow0 + rb;
+            double va = col_c[ra], vb = hb ? col_c[rb] : 0.0;
+            if (app) {
+#pragma unroll
+              for (int j = 0; j < GS; ++j) {
+                if ((live >> j) & 1u) {
+                  const double* vj = S + (size_t)(i + j) * LS;
+                  const double ea = ga > i + j ? vj[ra] : (ga == i + j ? 1.0 : 0.0);
+                  const double eb = gb > i + j ? (hb ? vj[rb] : 0.0) : (gb == i + j ? 1.0 : 0.0);
+                  va = fma(-ea, twv[j], va);
+                  vb = fma(-eb, twv[j], vb);
+                }
+              }
+              col_c[ra] = va;
+              if (hb) col_c[rb] = vb;
+            }
+            if (pub) {
+              if ((unsigned)(ra - pr0) < (unsigned)s2) pubrow[(size_t)(ra - pr0) * (QRDM_NB_MAX + 2) + c] = va;
+              if (hb && (unsigned)(rb - pr0) < (unsigned)s2) pubrow[(size_t)(rb - pr0) * (QRDM_NB_MAX + 2) + c] = vb;
+            }
+#pragma unroll
+            for (int k = 0; k < GS; ++k) {
+              if (k < s2 && c >= i2 + k) {
+                const double* xk = S + (size_t)(i2 + k) * LS;
+                const double xa = ga > i2 + k ? xk[ra] : 0.0;
+                const double xb = (hb && gb > i2 + k) ? xk[rb] : 0.0;
+                dacc[k] = fma(xb, vb, fma(xa, va, dacc[k]));
+              }
+            }
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < GS; ++k) {
+          if (k < s2) {
+            double v = dacc[k];
+            for (int o = 1; o < P; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+            if (part == 0 && cc < nc && c >= i2 + k && nr > 0) {
+              if ((abs_bits(v) >> 52) >= 1023ull + 16ull) atomicOr(&p.st->err, QRDM_EDEV_PANEL_RANGE);
+              else limbs_add(v, tot2 + (size_t)kLimbs * (k * fjb + c));
+            }
+          }
+        }
+      }
+    }
+    PPH(10);
+    __syncthreads();
+    PPH(6);
+    if (sm.flag == 1) {
+      done = i2;
+      break;
+    }
+    i = i2;
+  }
+  if (prof) {
+    pc[7] = (unsigned long long)(clock64() - tstart);
+    for (int k = 0; k < kPanelPhases; ++k) atomicAdd(p.prof + k, pc[k]);
+  }
+#undef PPH
+  if (!ok) return;
+  const int kc = done;
+  for (int e = tid; e < fjb * nr; e += blockDim.x) {
+    int c = e / nr, rr = e % nr;
+    int grow = grow0 + rr;
+    double v = S[(size_t)c * LS + rr];
+    if (!(c < kc && grow > c)) v = v / sm.sc[c];
+    W0[(size_t)c * lda + grow] = v;
+  }
+  double* vp = p.vtv_part + (size_t)g * QRDM_NB_MAX * QRDM_NB_MAX;
+  int npair = p.skip_vtv ? 0 : kc * (kc - 1) / 2;
+  for (int t = tid; t < npair; t += blockDim.x) {
+    int b = (int)((1.0 + sqrt(1.0 + 8.0 * (double)t)) * 0.5);
+    while (b * (b - 1) / 2 > t) --b;
+    while ((b + 1) * b / 2 <= t) ++b;
+    int a = t - b * (b - 1) / 2;
+    const double* va = S + (size_t)a * LS;
+    const double* vb = S + (size_t)b * LS;
+    double acc2 = 0.0;
+    int rstart = b - grow0;
+    if (rstart < 0) rstart = 0;
+    for (int rr = rstart; rr < nr; ++rr) {
+      int grow = grow0 + rr;
+      double y = (grow == b) ? 1.0 : vb[rr];
+      acc2 = fma(va[rr], y, acc2);
+    }
+    vp[a * QRDM_NB_MAX + b] = acc2;
+  }
+  if (g == 0 && tid == 0) p.st->fjb_cmp = kc;
+}
+
+// Launch the integer-total panel (cooperative) on G CTAs with `group`
+// columns per grid barrier (1: k_panel_red; 2, 4, 8: k_panel_grp); returns
+// the CUDA error of the launch.
+static const void* panel_kernel(int group);
+cudaError_t launch_panel_red(const PanelArgs& pa, int G, size_t smem, int group, cudaStream_t s) {
+  void* args[] = {const_cast<PanelArgs*>(&pa)};
+  return cudaLaunchCooperativeKernel(panel_kernel(group), dim3(G), dim3(256), args, smem, s);
+}
+
+// CTAs of that panel kernel that fit on one SM with this dynamic shared
+// memory (0 if it cannot run).
+int panel_red_per_sm(size_t smem, int group) {
   int n = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_panel_red, 256, smem) != cudaSuccess) {
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, panel_kernel(group), 256, smem) != cudaSuccess) {
     cudaGetLastError();
     return 0;
   }
   return n;
+}
+
+static const void* panel_kernel(int group) {
+  return group == 8   ? (const void*)k_panel_grp<8>
+         : group == 4 ? (const void*)k_panel_grp<4>
+         : group == 2 ? (const void*)k_panel_grp<2>
+                      : (const void*)k_panel_red;
+}
+
+// Static shared memory of the integer-total panel kernel for `group`
+// (queried once per kernel; callers hold the library lock).
+size_t panel_static_smem(int group) {
+  static size_t cached[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const int gi = (group == 2 || group == 4 || group == 8) ? group : 1;
+  if (cached[gi] == 0) {
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, panel_kernel(gi)) != cudaSuccess) {
+      cudaGetLastError();
+      return 0;
+    }
+    cached[gi] = fa.sharedSizeBytes;
+  }
+  return cached[gi];
+}
+
+// Dynamic shared memory limits of the panel kernels: the opt-in maximum
+// less each kernel's static shared memory.
+int panel_set_attributes(int big) {
+  int r = 0;
+  r |= cudaFuncSetAttribute(k_panel, cudaFuncAttributeMaxDynamicSharedMemorySize, big - 8192) != cudaSuccess;
+  const int groups[] = {1, 2, 4, 8};
+  for (int grp : groups) {
+    const size_t st = panel_static_smem(grp);
+    if (st == 0 || st + 1024 > (size_t)big) return 1;
+    r |= cudaFuncSetAttribute(panel_kernel(grp), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              big - (int)st - 1024) != cudaSuccess;
+  }
+  return r;
 }
 
 // Reset the block record and set the block's column counts (used by the
