@@ -617,7 +617,7 @@ __global__ void __launch_bounds__(256) k_panel_red(PanelArgs p) {
 // orthogonality depends on its column's squared norm relative to those
 // errors, so a group ends early (the next one starts with exact totals at
 // that column) when the earlier reflectors of the group have taken more than
-// 15/16 of the column's square; the corrected sums are then within ~16 x a
+// 3/4 of the column's square; the corrected sums are then within ~4 x a
 // few units of the exact ones.
 //
 // Per step the scalar chain is short: one rsqrt gives |beta| = s rsqrt(s)
@@ -631,8 +631,9 @@ struct PanelGrpSmem {
   double row[2][GS][QRDM_NB_MAX];  // rows i .. i+GS-1 of columns i .. fjb-1 (two states)
   double tw[GS][QRDM_NB_MAX];      // tau_j w_c of the group's reflectors
   double dy[GS], dv[GS];           // per step: x.(column i+k) and x.x over r > i+k, unscaled by scal
+  double twk[GS], Ck[GS];          // per step: tau w of column i+k, and v.(column i+k) - twk v.v
   double P0[GS], R0[GS];           // column i+k's totals and diagonal entry before the corrections
-  double M[GS];                    // 1/16 of column i+k's square at the group's start
+  double M[GS];                    // 1/4 of column i+k's square at the group's start
   double scal[GS], beta[GS], tau[GS], rbeta[GS];
   int tz[GS];
   double thres;
@@ -821,51 +822,57 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
         // sign(alpha) (|beta| - |alpha|) / |x|^2 with 1/|x|^2 taken beside
         // the rsqrt when |x|^2 >= alpha^2 (then |beta| >= sqrt(2) |alpha|
         // and the difference loses at most two bits), else as the
-        // reciprocal of alpha - beta; the tests resolve meanwhile
+        // reciprocal of alpha - beta.  The tests compare the bit patterns
+        // of nonnegative doubles as integers (their order is the values')
+        // and the selects move bits, so only the chain uses the FP64 pipe.
         const double alpha = rw[j][col];
-        double red0 = sm.P[j][col];
-        red0 = red0 < 0.0 ? 0.0 : red0;  // a corrected square can round below zero
+        const long long ab = __double_as_longlong(alpha);
+        long long r0b = __double_as_longlong(sm.P[j][col]);
+        r0b = r0b < 0 ? 0ll : r0b;  // a corrected square can round below zero (or be -0)
+        const double red0 = __longlong_as_double(r0b);
         const double s2 = fma(alpha, alpha, red0);
         const double r = rsqrt(s2);
-        const double aa = fabs(alpha);
-        int fl = 0, tz = 1;
-        if (j > 0 && s2 < sm.M[j]) {
-          // the group's earlier reflectors took more than 15/16 of this
-          // column's square: its corrected sums have lost too many bits,
-          // so the group ends here and the next one starts from exact
-          // totals at this column
-          fl = 3;
-        } else if (p.mloc - col > 1) {
-          const double t = sm.thres * sm.sc[col];
-          if (col > 0 && p.allow_exit && red0 < t * t) fl = 1;
-          else if (red0 != 0.0) tz = 0;
-        }
+        const double t = sm.thres * sm.sc[col];
+        long long t2b = __double_as_longlong(t * t);
+        t2b = t2b > 0x7FF0000000000000ll ? 0ll : t2b;  // a NaN threshold exits nothing
+        const long long sgn = (ab < 0 && ab != (long long)0x8000000000000000ull) ? 0ll : (long long)0x8000000000000000ull;
+        // sgn: the sign bit of -sign(alpha) (alpha = -0 counts as positive)
+        // trunc: the group's earlier reflectors took more than 3/4 of this
+        // column's square, so its corrected sums have lost too many bits;
+        // the group ends here and the next one starts from exact totals at
+        // this column
+        const bool trunc = j > 0 && __double_as_longlong(s2) < __double_as_longlong(sm.M[j]);
+        const bool order = p.mloc - col > 1;
+        const bool ex = !trunc && order && col > 0 && p.allow_exit && r0b < t2b;
+        const int fl = trunc ? 3 : (ex ? 1 : 0);
+        const int tz = (fl != 0 || !order || r0b == 0) ? 1 : 0;
         if (tid == 0) {
+          const double mag = s2 * r;  // |beta|
+          const double tau = fma(fabs(alpha), r, 1.0);  // (beta - alpha) / beta
+          const double beta = tz ? alpha : __longlong_as_double(__double_as_longlong(mag) ^ sgn);
+          const double rb = tz ? 0.0 : __longlong_as_double(__double_as_longlong(r) ^ sgn);  // 1 / beta
           if (fl) {
             sm.flag = fl;
           } else {
-            const double mag = s2 * r;  // |beta|
-            const double beta = tz ? alpha : (alpha >= 0.0 ? -mag : mag);
-            const double rb = tz ? 0.0 : (alpha >= 0.0 ? -r : r);  // 1 / beta
-            const double tau = tz ? 0.0 : fma(aa, r, 1.0);          // (beta - alpha) / beta
             if (col == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(beta) * sm.sc_inv[0];
             sm.beta[j] = beta;
             sm.tz[j] = tz;
-            sm.tau[j] = tau;
+            sm.tau[j] = tz ? 0.0 : tau;
             sm.rbeta[j] = rb;
-            if (g == 0) p.tau[col] = tau;
           }
         } else {
           const double ir0 = __drcp_rn(red0);
-          if (!tz && !fl) {
-            const double mag = s2 * r;
-            double sc_ = red0 >= alpha * alpha ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
-            sm.scal[j] = alpha >= 0.0 ? sc_ : -sc_;
+          const double mag = s2 * r;
+          const double aa = fabs(alpha);
+          if (!tz) {
+            const double sc_ = r0b >= __double_as_longlong(alpha * alpha) ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
+            // sign(alpha) / (|alpha| + |beta|): the sign bit of sign(alpha)
+            sm.scal[j] = __longlong_as_double(__double_as_longlong(sc_) ^ (sgn ^ (long long)0x8000000000000000ull));
           }
         }
       } else if (j == 0 && tid >= 192 && tid - 192 < s) {
         const int k = tid - 192;
-        sm.M[k] = 0.0625 * fma(sm.R0[k], sm.R0[k], sm.P0[k]);
+        sm.M[k] = 0.25 * fma(sm.R0[k], sm.R0[k], sm.P0[k]);
       } else if (tid >= 224 && tid - 224 < s - 1 - j) {
         const int k = j + 1 + (tid - 224);
         double dy = sm.P[j][i + k], dv = sm.P[j][col];
@@ -884,44 +891,52 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
         na = j;
         break;
       }
+      // (CTA 0 stores tau from a warp off the scalar chain: the chain's
+      // thread would wait behind the partials' atomics in the memory queue)
+      if (g == 0 && tid == 192) p.tau[col] = sm.tau[j];
       if (sm.tz[j]) continue;  // H(col) = I: nothing changes
-      // B. tau w_c of H(col); the later group columns' partials and rows
-      //    brought to the state after H(col) (rows into the other buffer)
+      // B. tau w_c of H(col) (and, beside it, the per-column constants of
+      //    the corrections); then the later group columns' partials and
+      //    rows brought to the state after H(col) (rows into the other
+      //    buffer):  P_k(c) -= tw_c (Y_k - tw_k V_k) + tw_k Z_kc  with
+      //    Y_k = v.(column i+k), V_k = v.v, Z_kc = v.(column c), r > i+k
       {
         const double tau = sm.tau[j], rb = sm.rbeta[j], scal = sm.scal[j];
-        double(*rn)[QRDM_NB_MAX] = sm.row[cur ^ 1];
         const int w1 = fjb - col - 1;  // columns after col
         const int nk = s - 1 - j;      // later group columns
-        const int npr = nk * w1 - nk * (nk - 1) / 2;
-        const int nrw = nk * w1;
-        const int ntot = npr + nrw + (nk == 0 ? w1 : 0);
-        for (int q = tid; q < ntot; q += blockDim.x) {
-          if (q < npr) {
-            int k = j + 1, rem = q;
-            while (rem >= fjb - i - k) {
-              rem -= fjb - i - k;
-              ++k;
+        if (tid < w1) {
+          const int c = col + 1 + tid;
+          sm.tw[j][c] = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
+        } else if (tid >= 224 && tid - 224 < nk) {
+          const int k = j + 1 + (tid - 224);
+          const double twk = grp_tw(tau, rb, rw[j][i + k], sm.P[j][i + k]);
+          const double Y = scal * sm.dy[k], V = (scal * scal) * sm.dv[k];
+          sm.twk[k] = twk;
+          sm.Ck[k] = fma(-twk, V, Y);
+        }
+        if (nk > 0) {
+          __syncthreads();
+          double(*rn)[QRDM_NB_MAX] = sm.row[cur ^ 1];
+          const int npr = nk * w1 - nk * (nk - 1) / 2;
+          const int nrw = nk * w1;
+          for (int q = tid; q < npr + nrw; q += blockDim.x) {
+            if (q < npr) {
+              int k = j + 1, rem = q;
+              while (rem >= fjb - i - k) {
+                rem -= fjb - i - k;
+                ++k;
+              }
+              const int c = i + k + rem;
+              double dz = sm.P[j][c];
+              for (int r = j + 1; r <= k; ++r) dz = fma(-rw[r][col], rw[r][c], dz);
+              double pn = fma(-sm.tw[j][c], sm.Ck[k], sm.P[k][c]);
+              pn = fma(-sm.twk[k], scal * dz, pn);
+              sm.P[k][c] = pn;
+            } else {
+              const int e = q - npr, rk = j + 1 + e / w1, c = col + 1 + e % w1;
+              const double v = rw[rk][col] * scal;  // the operations of the slab update
+              rn[rk][c] = fma(-v, sm.tw[j][c], rw[rk][c]);
             }
-            const int c = i + k + rem;
-            const double twc = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
-            const double twk = grp_tw(tau, rb, rw[j][i + k], sm.P[j][i + k]);
-            double dz = sm.P[j][c];
-            for (int r = j + 1; r <= k; ++r) dz = fma(-rw[r][col], rw[r][c], dz);
-            const double Y = scal * sm.dy[k], V = (scal * scal) * sm.dv[k], Z = scal * dz;
-            double pn = sm.P[k][c];
-            pn = fma(-twc, Y, pn);
-            pn = fma(-twk, Z, pn);
-            pn = fma(twk * twc, V, pn);
-            sm.P[k][c] = pn;
-            if (k == j + 1) sm.tw[j][c] = twc;  // (k = j+1 covers every c > col once)
-          } else if (q < npr + nrw) {
-            const int e = q - npr, rk = j + 1 + e / w1, c = col + 1 + e % w1;
-            const double twc = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
-            const double v = rw[rk][col] * scal;  // the operations of the slab update
-            rn[rk][c] = fma(-v, twc, rw[rk][c]);
-          } else {
-            const int c = col + 1 + (q - npr - nrw);
-            sm.tw[j][c] = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
           }
         }
       }
@@ -1046,14 +1061,38 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
             }
           }
         }
+        if (P >= GS) {
+          // recursive halving over the low log2(GS) lane bits (each lane
+          // sends half of its sums and adds the partner's other half), then
+          // butterflies: lane `part` ends with the total of k = part % GS,
+          // and the lanes part < GS add them
 #pragma unroll
-        for (int k = 0; k < GS; ++k) {
-          if (k < s2) {
-            double v = dacc[k];
-            for (int o = 1; o < P; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-            if (part == 0 && cc < nc && c >= i2 + k && nr > 0) {
-              if ((abs_bits(v) >> 52) >= 1023ull + 16ull) atomicOr(&p.st->err, QRDM_EDEV_PANEL_RANGE);
-              else limbs_add(v, tot2 + (size_t)kLimbs * (k * fjb + c));
+          for (int l = 0, L = GS; L > 1; ++l, L >>= 1) {
+            const bool bit = (part >> l) & 1;
+#pragma unroll
+            for (int t = 0; t < L / 2; ++t) {
+              const double send = bit ? dacc[2 * t] : dacc[2 * t + 1];
+              const double keep = bit ? dacc[2 * t + 1] : dacc[2 * t];
+              dacc[t] = keep + __shfl_xor_sync(0xffffffffu, send, 1 << l);
+            }
+          }
+          double v = dacc[0];
+          for (int o = GS; o < P; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+          const int k = part & (GS - 1);
+          if (part < GS && k < s2 && cc < nc && c >= i2 + k && nr > 0) {
+            if ((abs_bits(v) >> 52) >= 1023ull + 16ull) atomicOr(&p.st->err, QRDM_EDEV_PANEL_RANGE);
+            else limbs_add(v, tot2 + (size_t)kLimbs * (k * fjb + c));
+          }
+        } else {
+#pragma unroll
+          for (int k = 0; k < GS; ++k) {
+            if (k < s2) {
+              double v = dacc[k];
+              for (int o = 1; o < P; o <<= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+              if (part == 0 && cc < nc && c >= i2 + k && nr > 0) {
+                if ((abs_bits(v) >> 52) >= 1023ull + 16ull) atomicOr(&p.st->err, QRDM_EDEV_PANEL_RANGE);
+                else limbs_add(v, tot2 + (size_t)kLimbs * (k * fjb + c));
+              }
             }
           }
         }

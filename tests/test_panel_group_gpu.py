@@ -2,7 +2,9 @@
 
 The grouped panel (k_panel_grp) takes the partials of a group's later
 columns from the exact totals of the group's start plus rank-one
-corrections; group 1 is the one-column-per-barrier panel (k_panel_red).
+corrections (a group ends early at a column that has lost more than 3/4 of
+its square to the group's earlier reflectors); group 1 is the
+one-column-per-barrier panel (k_panel_red).
 Each setting runs in its own process (the library reads the variable once).
 Bar: identical DM blocks and pivots wherever the oracle's decisions are
 separated (Gaussian), leading R within 64 n eps ||A||_F of group 1's, and
