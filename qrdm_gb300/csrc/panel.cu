@@ -706,8 +706,12 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
   const int G = gridDim.x, g = blockIdx.x, R = p.rows_per_cta;
   const int LS = R | 1;
   const int fjb = p.st->fjb;
-  const int grow0 = g * R;
-  const int nr = max(0, min(R, p.mloc - grow0));
+  // slabs of R rows counted from the bottom, so that the short one is CTA
+  // 0's: the CTA holding the panel's top rows does the group rows' extra
+  // work, and every CTA waits for it at each grid barrier
+  const int gs = p.mloc - (G - g) * R;
+  const int grow0 = max(0, gs);
+  const int nr = max(0, gs + R - grow0);
   const size_t lda = (size_t)p.lda;
   double* W0 = p.A + (size_t)p.j * lda + p.j;
   // limb totals: three regions of GS x fjb slots, used by groups in turn;
@@ -957,28 +961,27 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
     const int s2 = (sm.flag == 1 || i2 >= fjb) ? 0 : min(GS, fjb - i2);
     unsigned long long* tot2 = acc + (size_t)((gi + 1) % 3) * region;
     if (live) {
+      // branch-free per row (the CTA holding the group's rows would
+      // otherwise diverge, and every CTA waits for it at the grid barrier):
+      // ev[j] is reflector j's entry at this row, v below its diagonal row,
+      // 1 on it and 0 above (fma(-1, t, x) = x - t and fma(-0, t, x) = x
+      // exactly)
       for (int rr = tid; rr < nr; rr += blockDim.x) {
         const int grow = grow0 + rr;
-        double vr[GS];  // v_j at this row (0 on and above its diagonal row)
+        double ev[GS];
 #pragma unroll
         for (int k = 0; k < GS; ++k) {
-          vr[k] = 0.0;
+          ev[k] = 0.0;
           if (k < na) {
             double val = S[(size_t)(i + k) * LS + rr];
 #pragma unroll
-            for (int j = 0; j < k; ++j) {
-              if ((live >> j) & 1u) {
-                if (grow > i + j) val = fma(-vr[j], sm.tw[j][i + k], val);
-                else if (grow == i + j) val -= sm.tw[j][i + k];
-              }
-            }
+            for (int j = 0; j < k; ++j)
+              if ((live >> j) & 1u) val = fma(-ev[j], sm.tw[j][i + k], val);
             if ((live >> k) & 1u) {
-              if (grow > i + k) {
-                val *= sm.scal[k];
-                vr[k] = val;
-              } else if (grow == i + k) {
-                val = sm.beta[k];
-              }
+              const double scaled = val * sm.scal[k];
+              const bool below = grow > i + k, diag = grow == i + k;
+              ev[k] = below ? scaled : (diag ? 1.0 : 0.0);
+              val = below ? scaled : (diag ? sm.beta[k] : val);
             }
             S[(size_t)(i + k) * LS + rr] = val;
           }
@@ -986,12 +989,8 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
         for (int c = i2; c < i2 + s2; ++c) {
           double val = S[(size_t)c * LS + rr];
 #pragma unroll
-          for (int j = 0; j < GS; ++j) {
-            if ((live >> j) & 1u) {
-              if (grow > i + j) val = fma(-vr[j], sm.tw[j][c], val);
-              else if (grow == i + j) val -= sm.tw[j][c];
-            }
-          }
+          for (int j = 0; j < GS; ++j)
+            if ((live >> j) & 1u) val = fma(-ev[j], sm.tw[j][c], val);
           S[(size_t)c * LS + rr] = val;
         }
       }
