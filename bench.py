@@ -213,6 +213,22 @@ def fp64_rates():
     return FP64_RATES
 
 
+def legacy_mma_rates():
+    """Rates of the warp-level tensor-core MMA (the library's
+    qrdm_legacy_mma_rates): INT8 in TOP/s and FP16 in TFLOP/s.  This GPU's
+    tcgen05 MMA has no INT8 kind, so the INT8 figure bounds what INT8 digits
+    (exact INT32 accumulation) could reach against the FP16 digits the Ozaki
+    split runs on tcgen05."""
+    from qrdm_gb300 import lib
+
+    out = (C.c_double * 2)()
+    rc = lib().qrdm_legacy_mma_rates(out, 2)
+    if rc != 0:
+        return {}
+    return {"int8_mma_sync_tops": out[0], "fp16_mma_sync_tflops": out[1],
+            "tcgen05_kind_i8": "not accepted by the assembler for sm_103a"}
+
+
 def fp64_peak():
     """(TFLOP/s, description) of the FP64 roof: the best measured FP64 rate."""
     r = fp64_rates()
@@ -714,6 +730,7 @@ def run_ours(args):
             variants["phase_ms"] = phase
             variants["blocks"] = nblk
             variants["fp64_rates_tflops"] = fp64_rates()
+            variants["legacy_mma_rates"] = legacy_mma_rates()
             if args.workload == "lowrank16k" and args.configs:
                 variants["configs"] = other_configs(L, stream)
         cpu = None

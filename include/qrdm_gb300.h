@@ -162,6 +162,14 @@ int qrdm_panel_phase_cycles(unsigned long long* out, int nout);
  * reference); synchronises the device. */
 int qrdm_fp64_rates(double* out, int nout);
 
+/* Measured rates of the legacy warp-level tensor-core MMA (mma.sync) of the
+ * current GPU: out[0] = INT8 (s8 x s8 -> s32, m16n8k32) in TOP/s, out[1] =
+ * FP16 (f16 x f16 -> f32, m16n8k16) in TFLOP/s; same method as
+ * qrdm_fp64_rates.  On sm_103a the tcgen05 MMA has no INT8 kind, so these
+ * bound what INT8 digits could reach.  Instrumentation only (no
+ * counterpart in the reference); synchronises the device. */
+int qrdm_legacy_mma_rates(double* out, int nout);
+
 /* ------------------------------------------------------------------ QP3 */
 /* Replaces dgeqp3, src/dgeqp3.c:39-93 (LAPACK dgeqp3 semantics: one pivot
  * per column by largest partial norm, first index on ties; jpvt[j] != 0

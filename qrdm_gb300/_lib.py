@@ -48,6 +48,7 @@ SIGNATURES = {
     "qrdm_batched_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     "qrdm_panel_phase_cycles": (C.c_int, [C.POINTER(C.c_ulonglong), C.c_int]),
     "qrdm_fp64_rates": (C.c_int, [_pd, C.c_int]),
+    "qrdm_legacy_mma_rates": (C.c_int, [_pd, C.c_int]),
     "qrdm_apply_jpvt_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p,
                                       C.c_int]),
     "qrdm_norm_diff_dev": (C.c_int, [C.c_int, C.c_int, C.c_void_p, C.c_int, C.c_void_p, C.c_int,
