@@ -560,7 +560,7 @@ def run_ours(args):
         if pcy[7]:
             pnames = ["block_sync", "derive_wait", "grid_barrier", "totals", "scalars_wait", "apply",
                       "partials_wait", None, "scalars_own", "derive_own", "partials_own"]
-            phase["panel_cta0_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames) if nm}
+            phase["panel_cta_share"] = {nm: pcy[k] / pcy[7] for k, nm in enumerate(pnames) if nm}
         nblk = int(sti.nblocks)
         if prec == 0:
             # FP64 GEMMs against the best FP64 rate measured on this GPU

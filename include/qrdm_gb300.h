@@ -142,8 +142,9 @@ int dgeqrdm_batched_dev(int count, const int* m, const int* n, double* d_a, int*
  * lifetime.  Instrumentation only (no counterpart in the reference). */
 int qrdm_batched_phase_cycles(unsigned long long* out, int nout);
 
-/* Panel phase cycles of CTA 0 summed over the panels of the last DM-QR call
- * made with stats.timing = 1: out[0..7] = block barrier before the grid
+/* Panel phase cycles of one CTA (CTA 0 of the one-column-per-barrier panel,
+ * the last CTA of the grouped panel, whose slab is full) summed over the
+ * panels of the last DM-QR call made with stats.timing = 1: out[0..7] = block barrier before the grid
  * arrival, corrections of a column group's later partials (grouped panel;
  * 0 otherwise), grid barrier, reading the column totals, reflector
  * scalars, reflector application, next-column partials and their

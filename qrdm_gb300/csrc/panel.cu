@@ -747,7 +747,9 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
 
   int done = fjb;
   bool ok = true;
-  const bool prof = p.prof != nullptr && g == 0 && tid == 0;
+  // (the last CTA: a full slab, on the grid barrier's critical path; CTA 0's
+  // slab is the short one)
+  const bool prof = p.prof != nullptr && g == G - 1 && tid == 0;
   unsigned long long pc[kPanelPhases] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
   long long tlast = clock64();
   const long long tstart = tlast;
