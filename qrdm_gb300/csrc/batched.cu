@@ -1019,31 +1019,44 @@ __device__ void solve_one(const BatchArgs& a, int p, BatchShared<KB>& S, double*
         if (lane == 0) S.red[sl] = acc;
       }
       __syncthreads();
-      if (tid == 0) {
+      if (tid == 0 || tid == 32) {
+        // FP64 instructions are the latency here (one active lane holds the
+        // FP64 pipe as long as a full warp), so the chain is one rsqrt of
+        // the scaled (overflow-safe) s = alpha^2 + |x|^2: |beta| = s rsqrt(s)
+        // and tau = 1 + |alpha| / |beta| (thread 0), and thread 32 forms
+        // 1/(alpha - beta) = sign(alpha) (|beta| - |alpha|) / |x|^2 with
+        // 1/|x|^2 taken beside the rsqrt when |x|^2 >= alpha^2, else as a
+        // reciprocal.  The exit test |x| / sc < thres compares |x|^2 with
+        // (thres sc)^2 as bit patterns of nonnegative doubles.
         const double alpha = x[i] * sci;
-        S.tau_zero = 1;
-        S.tau = 0.0;
-        S.scal = 0.0;
-        S.beta = x[i];
-        if (mloc - i > 1) {
-          // one thread: FP64 instructions are the latency, so the exact
-          // power-of-two scale is undone by multiplication and beta is
-          // formed directly from the scaled (overflow-safe) sum of squares
-          const double xs = sqrt(S.red[0]);
-          const double sinv = S.sc_inv[i];
-          if (i > 0 && xs * sinv < S.thres) {
-            S.exit_flag = 1;
-          } else if (xs != 0.0) {
-            const double bs = -sign_of(sqrt(fma(alpha, alpha, S.red[0])), alpha);
-            S.tau = (bs - alpha) / bs;
-            S.scal = 1.0 / (alpha - bs);
-            S.beta = bs * sinv;
-            S.tau_zero = 0;
+        const double red0 = S.red[0];
+        const long long r0b = __double_as_longlong(red0) < 0 ? 0ll : __double_as_longlong(red0);
+        const double s2 = fma(alpha, alpha, red0);
+        const double r = rsqrt(s2);
+        const double t = S.thres * S.sc[i];
+        long long t2b = __double_as_longlong(t * t);
+        t2b = t2b > 0x7FF0000000000000ll ? 0ll : t2b;  // a NaN threshold exits nothing
+        const long long ab = __double_as_longlong(alpha);
+        const long long sgn = (ab < 0 && ab != (long long)0x8000000000000000ull) ? 0ll : (long long)0x8000000000000000ull;
+        const bool order = mloc - i > 1;
+        const bool ex = order && i > 0 && r0b < t2b;
+        const bool tz = !order || ex || r0b == 0;
+        if (tid == 0) {
+          const double mag = s2 * r;  // |beta|, scaled
+          S.exit_flag = ex ? 1 : 0;
+          S.tau_zero = tz ? 1 : 0;
+          S.tau = tz ? 0.0 : fma(fabs(alpha), r, 1.0);  // (beta - alpha) / beta
+          S.beta = tz ? x[i] : __longlong_as_double(__double_as_longlong(mag) ^ sgn) * S.sc_inv[i];
+          if (!ex) {
+            if (i == 0 && fjb > 1 && a.tau_rel > 0.0) S.thres = a.tau_rel * fabs(S.beta);
+            tau[j + i] = S.tau;
           }
-        }
-        if (!S.exit_flag) {
-          if (i == 0 && fjb > 1 && a.tau_rel > 0.0) S.thres = a.tau_rel * fabs(S.beta);
-          tau[j + i] = S.tau;
+        } else if (!tz) {
+          const double ir0 = __drcp_rn(red0);
+          const double mag = s2 * r;
+          const double aa = fabs(alpha);
+          const double sc_ = r0b >= __double_as_longlong(alpha * alpha) ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
+          S.scal = __longlong_as_double(__double_as_longlong(sc_) ^ (sgn ^ (long long)0x8000000000000000ull));
         }
       }
       __syncthreads();
