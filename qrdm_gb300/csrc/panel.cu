@@ -822,55 +822,52 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
       // A. scalars of column col: thread 0 the exit tests, beta, 1/beta and
       //    tau; thread 32 the same beta and 1/(alpha - beta); warp 7 the
       //    sums over the group rows that the corrections subtract
-      if (tid == 0 || tid == 32) {
-        // the chain is s -> rsqrt -> beta and tau = 1 + |alpha| / |beta|
-        // (thread 0); thread 32 forms 1/(alpha - beta) =
+      if (tid == 0 || tid == 32 || tid == 64) {
+        // thread 0 runs only the chain s -> rsqrt -> |beta|, 1/beta and
+        // tau = 1 + |alpha| / |beta|; thread 32 forms 1/(alpha - beta) =
         // sign(alpha) (|beta| - |alpha|) / |x|^2 with 1/|x|^2 taken beside
         // the rsqrt when |x|^2 >= alpha^2 (then |beta| >= sqrt(2) |alpha|
         // and the difference loses at most two bits), else as the
-        // reciprocal of alpha - beta.  The tests compare the bit patterns
-        // of nonnegative doubles as integers (their order is the values')
-        // and the selects move bits, so only the chain uses the FP64 pipe.
+        // reciprocal of alpha - beta; thread 64 decides meanwhile whether the
+        // reflector is taken (the tests compare bit patterns of nonnegative
+        // doubles as integers), and the consumers select on its flags
         const double alpha = rw[j][col];
         const long long ab = __double_as_longlong(alpha);
         long long r0b = __double_as_longlong(sm.P[j][col]);
         r0b = r0b < 0 ? 0ll : r0b;  // a corrected square can round below zero (or be -0)
         const double red0 = __longlong_as_double(r0b);
         const double s2 = fma(alpha, alpha, red0);
-        const double r = rsqrt(s2);
-        const double t = sm.thres * sm.sc[col];
-        long long t2b = __double_as_longlong(t * t);
-        t2b = t2b > 0x7FF0000000000000ll ? 0ll : t2b;  // a NaN threshold exits nothing
+        // the sign bit of -sign(alpha) (alpha = -0 counts as positive)
         const long long sgn = (ab < 0 && ab != (long long)0x8000000000000000ull) ? 0ll : (long long)0x8000000000000000ull;
-        // sgn: the sign bit of -sign(alpha) (alpha = -0 counts as positive)
-        // trunc: the group's earlier reflectors took more than 3/4 of this
-        // column's square, so its corrected sums have lost too many bits;
-        // the group ends here and the next one starts from exact totals at
-        // this column
-        const bool trunc = j > 0 && __double_as_longlong(s2) < __double_as_longlong(sm.M[j]);
-        const bool order = p.mloc - col > 1;
-        const bool ex = !trunc && order && col > 0 && p.allow_exit && r0b < t2b;
-        const int fl = trunc ? 3 : (ex ? 1 : 0);
-        const int tz = (fl != 0 || !order || r0b == 0) ? 1 : 0;
-        if (tid == 0) {
-          const double mag = s2 * r;  // |beta|
-          const double tau = fma(fabs(alpha), r, 1.0);  // (beta - alpha) / beta
-          const double beta = tz ? alpha : __longlong_as_double(__double_as_longlong(mag) ^ sgn);
-          const double rb = tz ? 0.0 : __longlong_as_double(__double_as_longlong(r) ^ sgn);  // 1 / beta
-          if (fl) {
-            sm.flag = fl;
-          } else {
-            if (col == 0 && fjb > 1 && p.tau_rel > 0.0) sm.thres = p.tau_rel * fabs(beta) * sm.sc_inv[0];
-            sm.beta[j] = beta;
-            sm.tz[j] = tz;
-            sm.tau[j] = tz ? 0.0 : tau;
-            sm.rbeta[j] = rb;
-          }
+        if (tid == 64) {
+          const double t = sm.thres * sm.sc[col];
+          long long t2b = __double_as_longlong(t * t);
+          t2b = t2b > 0x7FF0000000000000ll ? 0ll : t2b;  // a NaN threshold exits nothing
+          // trunc: the group's earlier reflectors took more than 3/4 of
+          // this column's square, so its corrected sums have lost too many
+          // bits; the group ends here and the next one starts from exact
+          // totals at this column
+          const bool trunc = j > 0 && __double_as_longlong(s2) < __double_as_longlong(sm.M[j]);
+          const bool order = p.mloc - col > 1;
+          const bool ex = !trunc && order && col > 0 && p.allow_exit && r0b < t2b;
+          if (trunc || ex) sm.flag = trunc ? 3 : 1;
+          else sm.tz[j] = (!order || r0b == 0) ? 1 : 0;
         } else {
-          const double ir0 = __drcp_rn(red0);
-          const double mag = s2 * r;
-          const double aa = fabs(alpha);
-          if (!tz) {
+          const double r = rsqrt(s2);
+          const double mag = s2 * r;  // |beta|
+          if (tid == 0) {
+            sm.beta[j] = __longlong_as_double(__double_as_longlong(mag) ^ sgn);
+            sm.rbeta[j] = __longlong_as_double(__double_as_longlong(r) ^ sgn);  // 1 / beta
+            sm.tau[j] = fma(fabs(alpha), r, 1.0);                                // (beta - alpha) / beta
+            if (col == 0 && fjb > 1 && p.tau_rel > 0.0) {
+              // (column 0 has no exit or early end: no reflector only when
+              // it has no rows below the diagonal or |x| = 0, beta = alpha)
+              const bool tz0 = !(p.mloc > 1) || r0b == 0;
+              sm.thres = p.tau_rel * (tz0 ? fabs(alpha) : mag) * sm.sc_inv[0];
+            }
+          } else {
+            const double ir0 = __drcp_rn(red0);
+            const double aa = fabs(alpha);
             const double sc_ = r0b >= __double_as_longlong(alpha * alpha) ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
             // sign(alpha) / (|alpha| + |beta|): the sign bit of sign(alpha)
             sm.scal[j] = __longlong_as_double(__double_as_longlong(sc_) ^ (sgn ^ (long long)0x8000000000000000ull));
@@ -899,8 +896,8 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
       }
       // (CTA 0 stores tau from a warp off the scalar chain: the chain's
       // thread would wait behind the partials' atomics in the memory queue)
-      if (g == 0 && tid == 192) p.tau[col] = sm.tau[j];
-      if (sm.tz[j]) continue;  // H(col) = I: nothing changes
+      if (g == 0 && tid == 192) p.tau[col] = sm.tz[j] ? 0.0 : sm.tau[j];
+      if (sm.tz[j]) continue;  // H(col) = I: nothing changes (tau 0)
       // B. tau w_c of H(col) (and, beside it, the per-column constants of
       //    the corrections); then the later group columns' partials and
       //    rows brought to the state after H(col) (rows into the other
