@@ -634,6 +634,7 @@ struct PanelGrpSmem {
   double twk[GS], Ck[GS];          // per step: tau w of column i+k, and v.(column i+k) - twk v.v
   double P0[GS], R0[GS];           // column i+k's totals and diagonal entry before the corrections
   double M[GS];                    // 1/4 of column i+k's square at the group's start
+  double next_alpha, next_sq;      // the next step's pivot and |x|^2 (scalar warps)
   double scal[GS], beta[GS], tau[GS], rbeta[GS];
   int tz[GS];
   double thres;
@@ -816,65 +817,70 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
     PPH(3);
     int na = s;   // reflectors of the group that are accepted
     int cur = 0;  // row buffer holding the current state
-    for (int j = 0; j < s; ++j) {
+    // Reflector scalars of group column j from its pivot alpha and |x|^2
+    // (bits r0b, clamped at zero: a corrected square can round below it),
+    // in three roles on three warps: role 0 the chain s -> rsqrt -> |beta|,
+    // 1/beta and tau = 1 + |alpha| / |beta|; role 1 1/(alpha - beta) =
+    // sign(alpha) (|beta| - |alpha|) / |x|^2 with 1/|x|^2 taken beside the
+    // rsqrt when |x|^2 >= alpha^2 (then |beta| >= sqrt(2) |alpha| and the
+    // difference loses at most two bits), else as the reciprocal of
+    // alpha - beta; role 2 whether the reflector is taken (the tests compare
+    // bit patterns of nonnegative doubles as integers).  Consumers select on
+    // role 2's flags.
+    auto scalar_role = [&](int role, int j, int col, double alpha, long long r0b) {
+      const long long ab = __double_as_longlong(alpha);
+      const double red0 = __longlong_as_double(r0b);
+      const double s2 = fma(alpha, alpha, red0);
+      // the sign bit of -sign(alpha) (alpha = -0 counts as positive)
+      const long long sgn = (ab < 0 && ab != (long long)0x8000000000000000ull) ? 0ll : (long long)0x8000000000000000ull;
+      if (role == 2) {
+        const double t = sm.thres * sm.sc[col];
+        long long t2b = __double_as_longlong(t * t);
+        t2b = t2b > 0x7FF0000000000000ll ? 0ll : t2b;  // a NaN threshold exits nothing
+        // trunc: the group's earlier reflectors took more than 3/4 of this
+        // column's square, so its corrected sums have lost too many bits;
+        // the group ends here and the next one starts from exact totals at
+        // this column
+        const bool trunc = j > 0 && __double_as_longlong(s2) < __double_as_longlong(sm.M[j]);
+        const bool order = p.mloc - col > 1;
+        const bool ex = !trunc && order && col > 0 && p.allow_exit && r0b < t2b;
+        if (trunc || ex) sm.flag = trunc ? 3 : 1;
+        else sm.tz[j] = (!order || r0b == 0) ? 1 : 0;
+      } else {
+        const double r = rsqrt(s2);
+        const double mag = s2 * r;  // |beta|
+        if (role == 0) {
+          sm.beta[j] = __longlong_as_double(__double_as_longlong(mag) ^ sgn);
+          sm.rbeta[j] = __longlong_as_double(__double_as_longlong(r) ^ sgn);  // 1 / beta
+          sm.tau[j] = fma(fabs(alpha), r, 1.0);                                // (beta - alpha) / beta
+          if (col == 0 && fjb > 1 && p.tau_rel > 0.0) {
+            // (column 0 has no exit or early end: no reflector only when it
+            // has no rows below the diagonal or |x| = 0, then beta = alpha)
+            const bool tz0 = !(p.mloc > 1) || r0b == 0;
+            sm.thres = p.tau_rel * (tz0 ? fabs(alpha) : mag) * sm.sc_inv[0];
+          }
+        } else {
+          const double ir0 = __drcp_rn(red0);
+          const double aa = fabs(alpha);
+          const double sc_ = r0b >= __double_as_longlong(alpha * alpha) ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
+          // sign(alpha) / (|alpha| + |beta|): the sign bit of sign(alpha)
+          sm.scal[j] = __longlong_as_double(__double_as_longlong(sc_) ^ (sgn ^ (long long)0x8000000000000000ull));
+        }
+      }
+    };
+    const int role = tid == 128 ? 0 : (tid == 160 ? 1 : (tid == 192 ? 2 : -1));
+    // A. scalars of group column j in the current state (roles on threads
+    //    128, 160, 192), beside them the sums over the group rows that the
+    //    corrections of step j subtract (warp 7) and, for j = 0, the
+    //    early-end bounds (warp 3); the caller synchronises
+    auto phase_a = [&](int j) {
       const int col = i + j;
       double(*rw)[QRDM_NB_MAX] = sm.row[cur];
-      // A. scalars of column col: thread 0 the exit tests, beta, 1/beta and
-      //    tau; thread 32 the same beta and 1/(alpha - beta); warp 7 the
-      //    sums over the group rows that the corrections subtract
-      if (tid == 0 || tid == 32 || tid == 64) {
-        // thread 0 runs only the chain s -> rsqrt -> |beta|, 1/beta and
-        // tau = 1 + |alpha| / |beta|; thread 32 forms 1/(alpha - beta) =
-        // sign(alpha) (|beta| - |alpha|) / |x|^2 with 1/|x|^2 taken beside
-        // the rsqrt when |x|^2 >= alpha^2 (then |beta| >= sqrt(2) |alpha|
-        // and the difference loses at most two bits), else as the
-        // reciprocal of alpha - beta; thread 64 decides meanwhile whether the
-        // reflector is taken (the tests compare bit patterns of nonnegative
-        // doubles as integers), and the consumers select on its flags
-        const double alpha = rw[j][col];
-        const long long ab = __double_as_longlong(alpha);
-        long long r0b = __double_as_longlong(sm.P[j][col]);
-        r0b = r0b < 0 ? 0ll : r0b;  // a corrected square can round below zero (or be -0)
-        const double red0 = __longlong_as_double(r0b);
-        const double s2 = fma(alpha, alpha, red0);
-        // the sign bit of -sign(alpha) (alpha = -0 counts as positive)
-        const long long sgn = (ab < 0 && ab != (long long)0x8000000000000000ull) ? 0ll : (long long)0x8000000000000000ull;
-        if (tid == 64) {
-          const double t = sm.thres * sm.sc[col];
-          long long t2b = __double_as_longlong(t * t);
-          t2b = t2b > 0x7FF0000000000000ll ? 0ll : t2b;  // a NaN threshold exits nothing
-          // trunc: the group's earlier reflectors took more than 3/4 of
-          // this column's square, so its corrected sums have lost too many
-          // bits; the group ends here and the next one starts from exact
-          // totals at this column
-          const bool trunc = j > 0 && __double_as_longlong(s2) < __double_as_longlong(sm.M[j]);
-          const bool order = p.mloc - col > 1;
-          const bool ex = !trunc && order && col > 0 && p.allow_exit && r0b < t2b;
-          if (trunc || ex) sm.flag = trunc ? 3 : 1;
-          else sm.tz[j] = (!order || r0b == 0) ? 1 : 0;
-        } else {
-          const double r = rsqrt(s2);
-          const double mag = s2 * r;  // |beta|
-          if (tid == 0) {
-            sm.beta[j] = __longlong_as_double(__double_as_longlong(mag) ^ sgn);
-            sm.rbeta[j] = __longlong_as_double(__double_as_longlong(r) ^ sgn);  // 1 / beta
-            sm.tau[j] = fma(fabs(alpha), r, 1.0);                                // (beta - alpha) / beta
-            if (col == 0 && fjb > 1 && p.tau_rel > 0.0) {
-              // (column 0 has no exit or early end: no reflector only when
-              // it has no rows below the diagonal or |x| = 0, beta = alpha)
-              const bool tz0 = !(p.mloc > 1) || r0b == 0;
-              sm.thres = p.tau_rel * (tz0 ? fabs(alpha) : mag) * sm.sc_inv[0];
-            }
-          } else {
-            const double ir0 = __drcp_rn(red0);
-            const double aa = fabs(alpha);
-            const double sc_ = r0b >= __double_as_longlong(alpha * alpha) ? (mag - aa) * ir0 : __drcp_rn(aa + mag);
-            // sign(alpha) / (|alpha| + |beta|): the sign bit of sign(alpha)
-            sm.scal[j] = __longlong_as_double(__double_as_longlong(sc_) ^ (sgn ^ (long long)0x8000000000000000ull));
-          }
-        }
-      } else if (j == 0 && tid >= 192 && tid - 192 < s) {
-        const int k = tid - 192;
+      if (role >= 0) {
+        const long long pb = __double_as_longlong(sm.P[j][col]);
+        scalar_role(role, j, col, rw[j][col], pb < 0 ? 0ll : pb);
+      } else if (j == 0 && tid >= 96 && tid - 96 < s) {
+        const int k = tid - 96;
         sm.M[k] = 0.25 * fma(sm.R0[k], sm.R0[k], sm.P0[k]);
       } else if (tid >= 224 && tid - 224 < s - 1 - j) {
         const int k = j + 1 + (tid - 224);
@@ -887,42 +893,77 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
         sm.dy[k] = dy;
         sm.dv[k] = dv;
       }
-      PPH(8);
-      __syncthreads();
-      PPH(4);
+    };
+    phase_a(0);
+    PPH(8);
+    __syncthreads();
+    PPH(4);
+    for (int j = 0; j < s; ++j) {
+      const int col = i + j;
+      double(*rw)[QRDM_NB_MAX] = sm.row[cur];
       if (sm.flag == 1 || sm.flag == 3) {
         na = j;
         break;
       }
       // (CTA 0 stores tau from a warp off the scalar chain: the chain's
       // thread would wait behind the partials' atomics in the memory queue)
-      if (g == 0 && tid == 192) p.tau[col] = sm.tz[j] ? 0.0 : sm.tau[j];
-      if (sm.tz[j]) continue;  // H(col) = I: nothing changes (tau 0)
-      // B. tau w_c of H(col) (and, beside it, the per-column constants of
-      //    the corrections); then the later group columns' partials and
-      //    rows brought to the state after H(col) (rows into the other
-      //    buffer):  P_k(c) -= tw_c (Y_k - tw_k V_k) + tw_k Z_kc  with
-      //    Y_k = v.(column i+k), V_k = v.v, Z_kc = v.(column c), r > i+k
-      {
-        const double tau = sm.tau[j], rb = sm.rbeta[j], scal = sm.scal[j];
-        const int w1 = fjb - col - 1;  // columns after col
-        const int nk = s - 1 - j;      // later group columns
-        if (tid < w1) {
-          const int c = col + 1 + tid;
-          sm.tw[j][c] = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
-        } else if (tid >= 224 && tid - 224 < nk) {
-          const int k = j + 1 + (tid - 224);
-          const double twk = grp_tw(tau, rb, rw[j][i + k], sm.P[j][i + k]);
-          const double Y = scal * sm.dy[k], V = (scal * scal) * sm.dv[k];
-          sm.twk[k] = twk;
-          sm.Ck[k] = fma(-twk, V, Y);
-        }
-        if (nk > 0) {
+      if (g == 0 && tid == 96) p.tau[col] = sm.tz[j] ? 0.0 : sm.tau[j];
+      if (sm.tz[j]) {
+        // H(col) = I (tau 0): nothing changes; the next column's scalars
+        // from the same state
+        if (j + 1 < s) {
+          phase_a(j + 1);
           __syncthreads();
+          PPH(4);
+        }
+        continue;
+      }
+      // B. tau w_c of H(col) and the per-column constants of the
+      //    corrections; then the later group columns' partials and rows
+      //    brought to the state after H(col) (rows into the other buffer):
+      //      P_k(c) -= tw_c (Y_k - tw_k V_k) + tw_k Z_kc
+      //    with Y_k = v.(column i+k), V_k = v.v, Z_kc = v.(column c) over
+      //    r > i+k.  During the second half threads 128, 160 and 192 form
+      //    the next column's pivot and square as these corrections do (the
+      //    same operations, from inputs read before the barrier between the
+      //    halves) and run its scalar roles, and warp 7 forms the next
+      //    step's sums over the group rows, so the next step needs no
+      //    phase A.
+      const double tau = sm.tau[j], rb = sm.rbeta[j], scal = sm.scal[j];
+      const int w1 = fjb - col - 1;  // columns after col
+      const int nk = s - 1 - j;      // later group columns
+      const int k1 = j + 1, c1 = col + 1;  // the next column (c1 = i + k1)
+      // inputs of the next step's roles and sums, read in the first half
+      double in_a = 0.0, in_b = 0.0, in_c = 0.0, in_d = 0.0, in_e = 0.0, in_f = 0.0, in_g = 0.0;
+      if (tid < w1) {
+        const int c = col + 1 + tid;
+        sm.tw[j][c] = grp_tw(tau, rb, rw[j][c], sm.P[j][c]);
+      } else if (tid >= 224 && tid - 224 < nk) {
+        const int k = j + 1 + (tid - 224);
+        const double twk = grp_tw(tau, rb, rw[j][i + k], sm.P[j][i + k]);
+        const double Y = scal * sm.dy[k], V = (scal * scal) * sm.dv[k];
+        sm.twk[k] = twk;
+        sm.Ck[k] = fma(-twk, V, Y);
+        if (tid - 224 < nk - 1) {  // the next step's partials of column k1, read before they change
+          in_a = sm.P[k1][c1];
+          in_b = sm.P[k1][i + k + 1];
+        }
+      } else if (nk > 0 && role >= 0) {
+        in_a = rw[j][c1];
+        in_b = sm.P[j][c1];
+        in_c = rw[k1][col];
+        in_d = rw[k1][c1];
+        in_e = sm.dy[k1];
+        in_f = sm.dv[k1];
+        in_g = sm.P[k1][c1];
+      }
+      if (nk > 0) {
+        __syncthreads();
+        if (tid < 128) {
           double(*rn)[QRDM_NB_MAX] = sm.row[cur ^ 1];
           const int npr = nk * w1 - nk * (nk - 1) / 2;
           const int nrw = nk * w1;
-          for (int q = tid; q < npr + nrw; q += blockDim.x) {
+          for (int q = tid; q < npr + nrw; q += 128) {
             if (q < npr) {
               int k = j + 1, rem = q;
               while (rem >= fjb - i - k) {
@@ -941,6 +982,49 @@ __global__ void __launch_bounds__(256) k_panel_grp(PanelArgs p) {
               rn[rk][c] = fma(-v, sm.tw[j][c], rw[rk][c]);
             }
           }
+        } else if ((tid >> 5) <= 6) {
+          // warps 4, 5, 6 (whole warps: the barrier below is warp-aligned):
+          // the next column's pivot and square, the row update and the
+          // correction of the pair (k1, c1) above operation for operation,
+          // formed once (thread 128) and shared at a barrier of these three
+          // warps, then the next column's scalar roles (lane 0 of each)
+          if (role == 0) {
+            const double tw1 = grp_tw(tau, rb, in_a, in_b);
+            const double alpha1 = fma(-(in_c * scal), tw1, in_d);
+            const double dz = fma(-in_c, in_d, in_b);
+            const double Y = scal * in_e, V = (scal * scal) * in_f;
+            const double ck = fma(-tw1, V, Y);
+            double pn = fma(-tw1, ck, in_g);
+            pn = fma(-tw1, scal * dz, pn);
+            sm.next_alpha = alpha1;
+            sm.next_sq = pn;
+          }
+          __syncwarp();
+          asm volatile("bar.sync 1, 96;" ::: "memory");
+          if (role >= 0) {
+            const long long pb = __double_as_longlong(sm.next_sq);
+            scalar_role(role, k1, c1, sm.next_alpha, pb < 0 ? 0ll : pb);
+          }
+        } else if (tid >= 224 && tid - 224 < nk - 1) {
+          // the next step's sums over the group rows (its warp-7 part of
+          // phase A), from the values the corrections above form
+          const int k = k1 + 1 + (tid - 224), ck = i + k;
+          auto pnext = [&](int x, double p_k1x) {  // next-state partial of column k1 with column x
+            const double dzx = fma(-rw[k1][col], rw[k1][x], sm.P[j][x]);
+            const double t = fma(-sm.tw[j][x], sm.Ck[k1], p_k1x);
+            return fma(-sm.twk[k1], scal * dzx, t);
+          };
+          auto rnext = [&](int r, int x) {  // next-state group row r of column x
+            return fma(-(rw[r][col] * scal), sm.tw[j][x], rw[r][x]);
+          };
+          double dy = pnext(ck, in_b), dv = pnext(c1, in_a);
+          for (int r = k1 + 1; r <= k; ++r) {
+            const double xr = rnext(r, c1);
+            dy = fma(-xr, rnext(r, ck), dy);
+            dv = fma(-xr, xr, dv);
+          }
+          sm.dy[k] = dy;
+          sm.dv[k] = dv;
         }
       }
       PPH(9);
