@@ -35,7 +35,7 @@ if sys.argv[4] == "dgeqrf":
     out["info"] = np.array([QRF(102, A.shape[0], A.shape[1], A, A.shape[0], tau)])
     out["A"], out["tau"] = A, tau
 else:
-    r = qrdm_gb300.dgeqrdm(A0, nb=int(d["nb"]), precision=sys.argv[4])
+    r = qrdm_gb300.dgeqrdm(A0, nb=int(d["nb"]), tau_=float(d["tau_"]), precision=sys.argv[4])
     for k in ("A", "tau", "jpvt", "ncols"):
         out[k] = r[k]
     out["info"] = np.array([r["info"]])
@@ -43,10 +43,10 @@ np.savez(sys.argv[3], **out)
 """
 
 
-def _run(tmp_path, A0, group, what, nb=64):
-    inp = tmp_path / f"in_{group}_{what}.npz"
-    outp = tmp_path / f"out_{group}_{what}.npz"
-    np.savez(inp, A=A0, nb=np.int64(nb))
+def _run(tmp_path, A0, group, what, nb=64, tau_=0.15):
+    inp = tmp_path / f"in_{group}_{what}_{nb}.npz"
+    outp = tmp_path / f"out_{group}_{what}_{nb}.npz"
+    np.savez(inp, A=A0, nb=np.int64(nb), tau_=np.float64(tau_))
     env = dict(os.environ, QRDM_PANEL_GROUP=str(group))
     subprocess.run([sys.executable, "-c", _RUNNER, ROOT, str(inp), str(outp), what], env=env,
                    check=True, timeout=600)
@@ -111,3 +111,36 @@ def test_groups_unpivoted_rank_deficient(gpu_lib, tmp_path):
         r = _run(tmp_path, A0, g, "dgeqrf")
         assert int(r["info"][0]) == 0
         _bounds(A0, r, pivoted=False)
+
+
+@pytest.mark.gpu
+def test_groups_block_width_128(gpu_lib, tmp_path):
+    """DM blocks of up to 128 columns (the widest the device path takes):
+    the grouped panel's slabs and totals at their largest."""
+    from qrdm_gb300 import workloads as W
+
+    A0 = W.gaussian(3000, 1500, seed=74)
+    base = _run(tmp_path, A0, 1, "mixed", nb=128)
+    an = np.linalg.norm(A0)
+    for g in (1, 4):
+        r = base if g == 1 else _run(tmp_path, A0, g, "mixed", nb=128)
+        assert int(r["info"][0]) == 0
+        assert np.array_equal(r["ncols"], base["ncols"]) and np.array_equal(r["jpvt"], base["jpvt"]), g
+        dR = np.linalg.norm(np.triu(r["A"][:1500]) - np.triu(base["A"][:1500]))
+        assert dR <= 64 * 1500 * EPS * an, (g, dR / an)
+        _bounds(A0, r)
+
+
+@pytest.mark.gpu
+def test_groups_no_early_exit_graded(gpu_lib, tmp_path):
+    """tau_ = 0 (no early exit) on 1200 x 1200 with singular values down to
+    1e-12: inside a panel columns lose most of their norm, so groups end
+    early, and the factorisation stays within the bounds for every group
+    size."""
+    from qrdm_gb300 import workloads as W
+
+    A0 = W.graded_svd(1200, seed=75)
+    for g in (1, 4, 8):
+        r = _run(tmp_path, A0, g, "fp64", tau_=0.0)
+        assert int(r["info"][0]) == 0
+        _bounds(A0, r)
