@@ -431,16 +431,16 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       if (mixed && km == 64) {
         int rows_per_chunk = std::max(64, ceil_div(ceil_div(mloc, max_chunks), 64) * 64);
         int nchunk = ceil_div(mloc, rows_per_chunk);
-        k_gram_bf16<<<nchunk, 128, 0, s>>>(P.A, lda, j, mloc, rows_per_chunk, c.cand.as<Cand>(), d_st,
-                                           c.gram_part.as<double>());
+        CK(launch_pdl(k_gram_bf16, dim3(nchunk), dim3(128), 0, s, P.A, lda, j, mloc, rows_per_chunk,
+                      c.cand.as<Cand>(), d_st, c.gram_part.as<double>()));
         RET(check_launch());
-        k_gram_reduce_bf16<<<ceil_div(8 * km * km, 256), 256, 0, s>>>(
-            reinterpret_cast<const float*>(c.gram_part.as<double>()), nchunk, km, c.cand.as<Cand>(), d_st,
-            c.gram.as<double>());
+        CK(launch_pdl(k_gram_reduce_bf16, dim3(ceil_div(8 * km * km, 256)), dim3(256), 0, s,
+                      reinterpret_cast<const float*>(c.gram_part.as<double>()), nchunk, km, c.cand.as<Cand>(),
+                      d_st, c.gram.as<double>()));
         RET(check_launch());
         const int npair = kmax * (kmax - 1) / 2;
-        k_gram_recheck<<<std::max(1, ceil_div(npair * 32, 256)), 256, 0, s>>>(
-            P.A, lda, j, mloc, c.cand.as<Cand>(), P.delta, P.gram_margin, km, d_st, c.gram.as<double>());
+        CK(launch_pdl(k_gram_recheck, dim3(std::max(1, ceil_div(npair * 32, 256))), dim3(256), 0, s, P.A, lda, j,
+                      mloc, c.cand.as<Cand>(), P.delta, P.gram_margin, km, d_st, c.gram.as<double>()));
         RET(check_launch());
       } else {
         int rows_per_chunk = std::max(32, ceil_div(mloc, max_chunks));
@@ -459,12 +459,13 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
                     sizeof(unsigned) * ((size_t)ceil_div(nloc, 32) + 4) + sizeof(double) * (size_t)kmax * (kmax + 1) +
                     sizeof(unsigned long long) * 2 * (size_t)kmax + 64;
       if (smem + 1024 > c.smem_optin) return QRDM_ERR_UNSUPPORTED;
-      k_dm_pick<<<1, 256, smem, s>>>(c.cand.as<Cand>(), c.gram.as<double>(), km, nloc, kmax, P.delta,
-                                     P.jpvt + j, nrm + j, c.perm.as<int2>(), d_st);
+      CK(launch_pdl(k_dm_pick, dim3(1), dim3(256), smem, s, c.cand.as<Cand>(), c.gram.as<double>(), km, nloc,
+                    kmax, P.delta, P.jpvt + j, nrm + j, c.perm.as<int2>(), d_st));
       RET(check_launch());
       int max_entries = 2 * msw;
       size_t psm = sizeof(double) * 32 * (size_t)max_entries;
-      k_permute_columns<<<ceil_div(m, 32), 256, psm, s>>>(P.A, lda, m, j, c.perm.as<int2>(), d_st, max_entries);
+      CK(launch_pdl(k_permute_columns, dim3(ceil_div(m, 32)), dim3(256), psm, s, P.A, lda, m, j,
+                    c.perm.as<int2>(), d_st, max_entries));
       RET(check_launch());
     }
     PH(1);
@@ -522,10 +523,12 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
     PH(4);
     // ---- partial-norm downdate with recompute safeguard (norm_update)
     {
-      k_norm_downdate<<<ceil_div(nloc, 32), 128, 0, s>>>(P.A, lda, j, n, nrm, nrm_exact, c.list.as<int>(), d_st);
+      CK(launch_pdl(k_norm_downdate, dim3(ceil_div(nloc, 32)), dim3(128), 0, s, P.A, lda, j, n, nrm, nrm_exact,
+                    c.list.as<int>(), d_st));
       RET(check_launch());
       int blocks = std::min(ceil_div(nloc, 8), 4 * nsm);
-      k_norm_recompute<<<std::max(1, blocks), 256, 0, s>>>(P.A, lda, j, m, c.list.as<int>(), nrm, nrm_exact, d_st);
+      CK(launch_pdl(k_norm_recompute, dim3(std::max(1, blocks)), dim3(256), 0, s, P.A, lda, j, m,
+                    c.list.as<int>(), nrm, nrm_exact, d_st));
       RET(check_launch());
     }
     PH(5);

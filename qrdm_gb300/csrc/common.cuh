@@ -3,6 +3,38 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <utility>
+
+// Programmatic dependent launch.  A kernel launched by launch_pdl waits at
+// QRDM_PDL_ENTRY until the kernels before it in the stream have completed
+// and their writes are visible (for an ordinary launch the wait returns at
+// once), then lets the next such kernel be scheduled, whose blocks in turn
+// wait at its own entry: the launch of each kernel overlaps the end of the
+// one before instead of following it.
+#define QRDM_PDL_ENTRY()                                   \
+  do {                                                     \
+    asm volatile("griddepcontrol.wait;" ::: "memory");     \
+    asm volatile("griddepcontrol.launch_dependents;" ::); \
+  } while (0)
+
+namespace qrdm {
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_pdl(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+                              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kern, std::forward<Args>(args)...);
+}
+}  // namespace qrdm
+
 #ifndef QRDM_NB_MAX
 #define QRDM_NB_MAX 128  // largest DM block (nb) the device path accepts
 #endif

@@ -47,6 +47,7 @@ constexpr int kDowndateCols = 32;
 __global__ void __launch_bounds__(128) k_norm_downdate(const double* __restrict__ A, long long lda, int j, int n,
                                                        double* __restrict__ nrm, double* __restrict__ nrm_exact,
                                                        int* __restrict__ list, BlockState* st) {
+  QRDM_PDL_ENTRY();
   __shared__ double sr[kDowndateCols][QRDM_NB_MAX + 1];
   const int fjb_cmp = min(st->fjb_cmp, QRDM_NB_MAX);
   const int cb = j + fjb_cmp + blockIdx.x * kDowndateCols;
@@ -99,6 +100,7 @@ __global__ void __launch_bounds__(128) k_norm_downdate(const double* __restrict_
 __global__ void k_norm_recompute(const double* __restrict__ A, long long lda, int j, int m,
                                  const int* __restrict__ list, double* __restrict__ nrm,
                                  double* __restrict__ nrm_exact, BlockState* st) {
+  QRDM_PDL_ENTRY();
   int count = st->recompute;
   const int r0 = j + st->fjb_cmp;
   int warps = blockDim.x >> 5;

@@ -613,6 +613,7 @@ constexpr int NST2 = 2;  // W2 digit stages (a third one measured slower: its sh
 
 template <int S>
 __global__ void __launch_bounds__(OZ_G2_THREADS, 1) k_oz_gemm2(OzG2Args g) {
+  QRDM_PDL_ENTRY();
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* adig = base;              // S x 16 KB: V digits of one band

@@ -84,6 +84,7 @@ constexpr int kTopkList = 512;
 __global__ void __launch_bounds__(1024) k_topk_radix(const double* __restrict__ nrm, int count, int kmax,
                                                      double tau_rel, Cand* __restrict__ cand,
                                                      BlockState* __restrict__ st, int cached) {
+  QRDM_PDL_ENTRY();
   // cached: the keys are read from global memory once into shared memory
   // (count <= kTopkKeysMax), and every pass reads them there
   extern __shared__ unsigned long long s_keys[];
@@ -429,6 +430,7 @@ __global__ void k_gram_reduce(const double* __restrict__ part, int nchunk, int k
 __global__ void k_gram_reduce_bf16(const float* __restrict__ part, int nchunk, int km,
                                    const Cand* __restrict__ cand, const BlockState* __restrict__ st,
                                    double* __restrict__ gram) {
+  QRDM_PDL_ENTRY();
   int nc = st->nc;
   if (nc <= 1) return;
   const int gt = blockIdx.x * blockDim.x + threadIdx.x;
@@ -469,6 +471,7 @@ __global__ void __launch_bounds__(256) k_dm_pick(const Cand* __restrict__ cand,
                                                  int ncols, int kmax, double delta,
                                                  int* __restrict__ jpvt, double* __restrict__ nrm,
                                                  int2* __restrict__ perm, BlockState* st) {
+  QRDM_PDL_ENTRY();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   // layout: [stage doubles 2*maxsw][stage ints 2*maxsw][sel kmax][pos kmax]
   //         [swapA maxsw][swapB maxsw][bitmap ceil(ncols/32) words]
@@ -666,6 +669,7 @@ __global__ void __launch_bounds__(256) k_permute_columns(double* __restrict__ A,
                                                          const int2* __restrict__ perm,
                                                          const BlockState* __restrict__ st,
                                                          int max_entries) {
+  QRDM_PDL_ENTRY();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int ROWS = 32;
   double* s = reinterpret_cast<double*>(smem_raw);  // [max_entries][ROWS]
@@ -746,6 +750,7 @@ __global__ void __launch_bounds__(128) k_gram_bf16(const double* __restrict__ A,
                                                    int mloc, int rows_per_chunk,
                                                    const Cand* __restrict__ cand,
                                                    BlockState* __restrict__ st, double* __restrict__ part) {
+  QRDM_PDL_ENTRY();
   __shared__ __align__(1024) unsigned char tile[128 * 128];
   __shared__ int s_e[64];
   __shared__ int s_col[64];
@@ -834,6 +839,7 @@ __global__ void __launch_bounds__(256) k_gram_recheck(const double* __restrict__
                                                       int mloc, const Cand* __restrict__ cand,
                                                       double delta, double margin, int km,
                                                       BlockState* __restrict__ st, double* __restrict__ gram) {
+  QRDM_PDL_ENTRY();
   const int nc = st->nc;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
   const int npair = nc * (nc - 1) / 2;
