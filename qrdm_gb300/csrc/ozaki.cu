@@ -273,6 +273,7 @@ constexpr int OZ_G1_CPT = 256 / OZ_G1_CONV;            // drained reflector colu
 
 template <int S>
 __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
+  QRDM_PDL_ENTRY();
   extern __shared__ unsigned char smem_raw[];
   unsigned char* base = (unsigned char*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   unsigned char* adig = base;               // S x 16 KB: 128 C columns x 64 rows
@@ -481,6 +482,7 @@ __global__ void __launch_bounds__(OZ_G1_THREADS, 1) k_oz_gemm1(OzG1Args g) {
 // sum over the CTAs that covered tile 0, in CTA order, of W^T(b, a), a < b.
 __global__ void __launch_bounds__(256) k_oz_vtv(const double* __restrict__ Wp, int nchunk, int per, int mt,
                                                 const BlockState* __restrict__ st, double* __restrict__ vtv) {
+  QRDM_PDL_ENTRY();
   const int k = st->fjb_cmp;
   const int npair = k * (k - 1) / 2;
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -507,6 +509,7 @@ __global__ void __launch_bounds__(OZ_TPB) k_oz_w2(const double* __restrict__ Wp,
                                                    const double* __restrict__ T, int ldt, int ncols,
                                                    const BlockState* __restrict__ st,
                                                    unsigned char* __restrict__ wb2, int* __restrict__ wexp) {
+  QRDM_PDL_ENTRY();
   __shared__ double sW[OZ_W2_COLS][65];  // [c][a]
   __shared__ double sT[64][65];          // T(b, a) at [a][b]
   __shared__ double smax[OZ_W2_COLS];
@@ -818,9 +821,13 @@ static int oz_run(cudaStream_t st_, double* W0, long long lda, int mloc, int nco
   a1.mt = mt;
   k_oz_gemm1<S><<<grid, OZ_G1_THREADS, oz_gemm1_smem(S), st_>>>(a1);
   // T factor from the V^T V rows of W (dlarft 'F','C'), needed from here on
-  k_oz_vtv<<<ceil_div(ldt * (ldt - 1) / 2, 256) + 1, 256, 0, st_>>>(Wp, nchunk, per, mt, st, vtv);
+  if (launch_pdl(k_oz_vtv, dim3(ceil_div(ldt * (ldt - 1) / 2, 256) + 1), dim3(256), 0, st_, Wp, nchunk, per, mt,
+                 st, vtv) != cudaSuccess)
+    return 1;
   launch_larft(vtv, tau, st, T, ldt, st_);
-  k_oz_w2<S><<<ceil_div(ncols - 1, OZ_W2_COLS), OZ_TPB, 0, st_>>>(Wp, nchunk, per, mt, T, ldt, ncols, st, wb2, wexp);
+  if (launch_pdl(k_oz_w2<S>, dim3(ceil_div(ncols - 1, OZ_W2_COLS)), dim3(OZ_TPB), 0, st_, Wp, nchunk, per, mt, T,
+                 ldt, ncols, st, wb2, wexp) != cudaSuccess)
+    return 1;
   OzG2Args a2;
   a2.W0 = W0;
   a2.lda = lda;

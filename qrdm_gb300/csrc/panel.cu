@@ -1377,6 +1377,7 @@ __global__ void __launch_bounds__(32) k_larft(const double* __restrict__ vtv,
                                               const double* __restrict__ tau,
                                               const BlockState* __restrict__ st,
                                               double* __restrict__ T, int ldt) {
+  QRDM_PDL_ENTRY();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   const int k = st->fjb_cmp;
   const int j = blockIdx.x;
@@ -1428,7 +1429,7 @@ __global__ void __launch_bounds__(32) k_larft(const double* __restrict__ vtv,
 void launch_larft(const double* vtv, const double* tau, const BlockState* st, double* T, int kmax,
                   cudaStream_t s) {
   const size_t smem = sizeof(double) * ((size_t)kmax * (kmax - 1) / 2 + (size_t)kmax);
-  k_larft<<<kmax, 32, smem, s>>>(vtv, tau, st, T, kmax);
+  launch_pdl(k_larft, dim3(kmax), dim3(32), smem, s, vtv, tau, st, T, kmax);
 }
 
 }  // namespace qrdm
