@@ -270,7 +270,8 @@ static int fixed_columns(Ctx& c, int m, int n, double* d_a, long long lda, doubl
 // an SM's, since the scheduler would otherwise pack two CTAs onto some SMs
 // and double their FP64 work), else the plain cooperative kernel.
 // *G_used receives the number of CTAs (the count of V^T V partials).
-static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t s, int* G_used) {
+static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t s, int* G_used,
+                        bool prezeroed = false) {
   if (c.pan_smem_floor == 0) {
     int per_sm = 0;
     if (cudaDeviceGetAttribute(&per_sm, cudaDevAttrMaxSharedMemoryPerMultiprocessor, c.dev) != cudaSuccess)
@@ -294,8 +295,10 @@ static int launch_panel(Ctx& c, PanelArgs& pa, int mloc, int kmax, cudaStream_t 
       // k_panel_grp: its three group regions) and the barrier counter start
       // at zero
       const size_t ntot = group > 1 ? panel_grp_totals(kmax, group) : panel_red_totals(kmax);
-      CK(cudaMemsetAsync(pa.part, 0, sizeof(unsigned long long) * ntot, s));
-      CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
+      if (!prezeroed) {
+        CK(cudaMemsetAsync(pa.part, 0, sizeof(unsigned long long) * ntot, s));
+        CK(cudaMemsetAsync(pa.bar, 0, sizeof(unsigned) * 4, s));
+      }
       if (launch_panel_red(pa, G, smem, group, s) == cudaSuccess) {
         ++g_launches;
         *G_used = G;
@@ -464,8 +467,13 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       RET(check_launch());
       int max_entries = 2 * msw;
       size_t psm = sizeof(double) * 32 * (size_t)max_entries;
+      // (and the panel's limb totals and barrier counter zeroed, for
+      // whichever panel kernel runs)
+      const int zero_words = (int)std::max(panel_grp_totals(kmax, kPanelGroupMax), panel_red_totals(kmax));
       CK(launch_pdl(k_permute_columns, dim3(ceil_div(m, 32)), dim3(256), psm, s, P.A, lda, m, j,
-                    c.perm.as<int2>(), d_st, max_entries));
+                    c.perm.as<int2>(), d_st, max_entries,
+                    reinterpret_cast<unsigned long long*>(c.pan_part.as<double>()), zero_words,
+                    c.pan_bar.as<unsigned>()));
       RET(check_launch());
     }
     PH(1);
@@ -493,7 +501,7 @@ static int dmqr_run(Ctx& c, DmqrProblem& P, qrdm_stats* stats) {
       pa.skip_vtv = oz_block ? 1 : 0;
       pa.prof = timing ? c.pan_prof.as<unsigned long long>() : nullptr;
       pa.spin_limit = P.spin_limit;
-      RET(launch_panel(c, pa, mloc, kmax, s, &G));
+      RET(launch_panel(c, pa, mloc, kmax, s, &G, /*prezeroed=*/true));
     }
     PH(2);
     // ---- T factor (dlarft 'F','C', src/dgeqrdm_work.c:751-754); the mixed

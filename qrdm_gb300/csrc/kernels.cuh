@@ -85,7 +85,8 @@ __global__ void k_gram_recheck(const double* A, long long lda, int j, int mloc, 
 __global__ void k_dm_pick(const Cand* cand, const double* gram, int km, int ncols, int kmax,
                           double delta, int* jpvt, double* nrm, int2* perm, BlockState* st);
 __global__ void k_permute_columns(double* A, long long lda, int m, int j, const int2* perm,
-                                  const BlockState* st, int max_entries);
+                                  const BlockState* st, int max_entries, unsigned long long* zero,
+                                  int zero_words, unsigned* zero4);
 
 // panel.cu
 __global__ void k_block_init(BlockState* st, int fjb, int fjb_cmp);

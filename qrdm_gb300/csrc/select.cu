@@ -668,8 +668,14 @@ __global__ void __launch_bounds__(256) k_permute_columns(double* __restrict__ A,
                                                          int m, int j,
                                                          const int2* __restrict__ perm,
                                                          const BlockState* __restrict__ st,
-                                                         int max_entries) {
+                                                         int max_entries,
+                                                         unsigned long long* __restrict__ zero,
+                                                         int zero_words, unsigned* __restrict__ zero4) {
   QRDM_PDL_ENTRY();
+  // the panel that follows needs zeroed totals and barrier counter: cleared
+  // here instead of by separate memory sets between the two launches
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < zero_words; q += gridDim.x * blockDim.x) zero[q] = 0ull;
+  if (zero4 && blockIdx.x == 0 && threadIdx.x < 4) zero4[threadIdx.x] = 0u;
   extern __shared__ __align__(16) unsigned char smem_raw[];
   constexpr int ROWS = 32;
   double* s = reinterpret_cast<double*>(smem_raw);  // [max_entries][ROWS]
